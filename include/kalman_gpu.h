@@ -1,0 +1,108 @@
+/*
+ * kalman_gpu.h -- entry points that libukgpu.so adds beside the reference API
+ * of kalman.h.  None of them has a counterpart in UltimateKalman; each one
+ * exists because the GPU boundary needs it:
+ *
+ *  - error reporting: the reference aborts on errors (assert), a library on a
+ *    shared GPU must not;
+ *  - a batched entry over many independent tracks (one launch sequence for
+ *    thousands of smoothing problems);
+ *  - a device-resident entry that takes packed arrays already in GPU memory,
+ *    so a caller can keep inputs in HBM and skip the host marshalling.
+ *
+ * Packed layout (host or device arrays, FP64, column-major blocks):
+ *
+ *   steps of all tracks are concatenated; track t owns global steps
+ *   [track_start[t], track_start[t+1]).  The first step of every track has no
+ *   evolution equation: its H, F, c, K slots are ignored.
+ *
+ *   H, F       [nsteps][n*n]     evolution  H_i x_i = F_i x_{i-1} + c_i + e_i
+ *   c          [nsteps][n]
+ *   K          [nsteps][n*n]     covariance factor of e_i, type K_type[i]
+ *                                ('w': the first n entries hold the column)
+ *   G          [nsteps][mmax*n]  observation G_i x_i = o_i + d_i, ld = mmax
+ *   o          [nsteps][mmax]
+ *   C          [nsteps][mmax*mmax] covariance factor of d_i, ld = mmax,
+ *                                type C_type[i] ('w': first m_i entries)
+ *   obs_rows   [nsteps]          m_i, the rows of G_i; 0 = no observation
+ *   state      [nsteps][n]       output
+ *   covariance [nsteps][n*n]     output (may be NULL with KALMAN_NO_COVARIANCE)
+ *
+ * The covariance-type letters are those of kalman.h.
+ */
+#ifndef KALMAN_GPU_H
+#define KALMAN_GPU_H
+
+#include <stdint.h>
+#include "kalman.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes returned by the int-valued entry points and recorded for the
+ * void-valued reference entry points.                                        */
+enum {
+  KALMAN_GPU_OK        = 0,
+  KALMAN_GPU_EINVAL    = 1,  /* bad argument or unsupported shape            */
+  KALMAN_GPU_ECUDA     = 2,  /* CUDA runtime error                           */
+  KALMAN_GPU_ENOMEM    = 3,  /* device or pinned-host allocation failed      */
+  KALMAN_GPU_ESINGULAR = 4,  /* a zero pivot: the problem is not observable;
+                                affected outputs are NaN                     */
+  KALMAN_GPU_ENODEV    = 5   /* no CUDA device                               */
+};
+
+/* Option bit added to kalman_options_t: factor in FP32 and refine the
+ * estimates with FP64 residuals of the least-squares system.                 */
+#define KALMAN_GPU_FP32_REFINE (1u << 20)
+
+/* Last error of the calling thread: status code and a one-line message.     */
+int         kalman_gpu_last_status(void);
+const char* kalman_gpu_last_error(void);
+void        kalman_gpu_clear_error(void);
+
+typedef struct kalman_gpu_problem_st {
+  int32_t n;
+  int32_t mmax;
+  int32_t ntracks;
+  int32_t reserved;
+  int64_t nsteps;
+  const int64_t* track_start;   /* always a HOST array of ntracks+1 entries  */
+  const double*  H;
+  const double*  F;
+  const double*  c;
+  const double*  K;
+  const char*    K_type;
+  const double*  G;
+  const double*  o;
+  const double*  C;
+  const char*    C_type;
+  const int32_t* obs_rows;
+  double*        state;
+  double*        covariance;
+} kalman_gpu_problem_t;
+
+/* Odd-even (Gargir-Toledo) smoothing of every track of a packed problem whose
+ * arrays are in device memory, on the given CUDA stream (NULL: the legacy
+ * default stream).  Returns a status code; the call is asynchronous with
+ * respect to the host only after it has validated its arguments.            */
+int kalman_gpu_smooth_oddeven_packed    (uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream);
+/* Associative-scan (Sarkka-Garcia-Fernandez) smoothing of a packed problem.  */
+int kalman_gpu_smooth_associative_packed(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream);
+
+/* Batched form of kalman_smooth_oddeven / kalman_smooth_associative: the
+ * equations of ntracks independent tracks are stored one track after the
+ * other; track t has track_lengths[t] steps.  Results are written into the
+ * equations as the single-track entry points do.                            */
+int kalman_gpu_smooth_tracks(uint32_t options, kalman_step_equations_t** equations,
+                             const kalman_step_index_t* track_lengths, int32_t ntracks);
+
+/* Releases the device workspace and pinned staging buffers cached by the
+ * library for the current device.                                            */
+void kalman_gpu_release(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KALMAN_GPU_H */
