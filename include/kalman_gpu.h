@@ -61,11 +61,17 @@ int         kalman_gpu_last_status(void);
 const char* kalman_gpu_last_error(void);
 void        kalman_gpu_clear_error(void);
 
+/* Where the arrays of a kalman_gpu_problem_t live.  Host arrays are copied to
+ * the device and the outputs back inside the call (page-locked host memory
+ * makes the copies faster).                                                  */
+#define KALMAN_GPU_DEVICE 0
+#define KALMAN_GPU_HOST   1
+
 typedef struct kalman_gpu_problem_st {
   int32_t n;
   int32_t mmax;
   int32_t ntracks;
-  int32_t reserved;
+  int32_t location;             /* KALMAN_GPU_DEVICE or KALMAN_GPU_HOST     */
   int64_t nsteps;
   const int64_t* track_start;   /* always a HOST array of ntracks+1 entries  */
   const double*  H;
@@ -82,10 +88,11 @@ typedef struct kalman_gpu_problem_st {
   double*        covariance;
 } kalman_gpu_problem_t;
 
-/* Odd-even (Gargir-Toledo) smoothing of every track of a packed problem whose
- * arrays are in device memory, on the given CUDA stream (NULL: the legacy
- * default stream).  Returns a status code; the call is asynchronous with
- * respect to the host only after it has validated its arguments.            */
+/* Odd-even (Gargir-Toledo) smoothing of every track of a packed problem, on
+ * the given CUDA stream (NULL: the legacy default stream).  Returns a status
+ * code.  With device arrays the call returns once the work is queued on the
+ * stream, except that it waits for the stream to report singular pivots;
+ * with host arrays it returns when the outputs are back in host memory.     */
 int kalman_gpu_smooth_oddeven_packed    (uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream);
 /* Associative-scan (Sarkka-Garcia-Fernandez) smoothing of a packed problem.  */
 int kalman_gpu_smooth_associative_packed(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream);
@@ -96,6 +103,19 @@ int kalman_gpu_smooth_associative_packed(uint32_t options, const kalman_gpu_prob
  * equations as the single-track entry points do.                            */
 int kalman_gpu_smooth_tracks(uint32_t options, kalman_step_equations_t** equations,
                              const kalman_step_index_t* track_lengths, int32_t ntracks);
+
+/* Kernel timing.  While enabled (per host thread), each kernel launch of the
+ * smoothers is bracketed by CUDA events on its stream.  _read returns, per
+ * kernel class that ran since it was enabled, its name, summed time (ms) and
+ * launch count.                                                              */
+void    kalman_gpu_profile_enable(int on);
+int     kalman_gpu_profile_read(int max_kinds, const char** names, double* total_ms, int64_t* launches);
+/* Number of kernels this host thread has launched through the library.      */
+int64_t kalman_gpu_launch_count(void);
+/* Measures the FP64 fused-multiply-add throughput of the current device in
+ * TFLOP/s, with `active_lanes` (1..32) active threads per warp.  A diagnostic
+ * for roofline reporting; takes a few milliseconds.                          */
+double  kalman_gpu_measure_fp64_tflops(int active_lanes);
 
 /* Releases the device workspace and pinned staging buffers cached by the
  * library for the current device.                                            */

@@ -33,7 +33,7 @@ KALMAN_NO_COVARIANCE = 1 << 16
 class ProblemStruct(ctypes.Structure):
     """ctypes image of kalman_gpu_problem_t (include/kalman_gpu.h)."""
     _fields_ = [
-        ("n", ctypes.c_int32), ("mmax", ctypes.c_int32), ("ntracks", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("n", ctypes.c_int32), ("mmax", ctypes.c_int32), ("ntracks", ctypes.c_int32), ("location", ctypes.c_int32),
         ("nsteps", ctypes.c_int64), ("track_start", ctypes.c_void_p),
         ("H", ctypes.c_void_p), ("F", ctypes.c_void_p), ("c", ctypes.c_void_p), ("K", ctypes.c_void_p),
         ("K_type", ctypes.c_void_p), ("G", ctypes.c_void_p), ("o", ctypes.c_void_p), ("C", ctypes.c_void_p),
@@ -52,7 +52,7 @@ def host_struct(P, state, cov):
         a = getattr(P, f)
         assert a.dtype == np.float64 and a.flags.c_contiguous, f
     s = ProblemStruct()
-    s.n, s.mmax, s.ntracks, s.reserved = P.n, P.mmax, P.ntracks, 0
+    s.n, s.mmax, s.ntracks, s.location = P.n, P.mmax, P.ntracks, 1
     s.nsteps = P.nsteps
     s.track_start = _ptr(P.track_start)
     s.H, s.F, s.c, s.K = _ptr(P.H), _ptr(P.F), _ptr(P.c), _ptr(P.K)

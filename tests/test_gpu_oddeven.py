@@ -1,0 +1,121 @@
+"""Parity of the CUDA odd-even smoother (through the C ABI) with the oracle,
+the reference's own outputs and the dense least-squares solution.
+
+Tolerance: 1e-11 relative error (normwise per step) for FP64 states and
+covariances, against the oracle and the reference."""
+import numpy as np
+import pytest
+
+import oracle
+from ultimate_kalman_gb300 import native, problem as pb
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-11
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    native.load()
+
+
+def check(P, X, S, tol=TOL, cov=True):
+    st, Xo, So = oracle.smooth(P, "oddeven", covariance=cov)
+    assert st == 0
+    assert oracle.rel_err_states(X, Xo) < tol
+    if cov:
+        assert oracle.rel_err_covs(S, So) < tol
+
+
+def test_golden_against_reference(golden):
+    P, d = golden
+    X, S = native.smooth(P, "oddeven")
+    ref = "oddeven" if "X_oddeven" in d else "ultimate"
+    assert oracle.rel_err_states(X, d[f"X_{ref}"]) < TOL
+    assert oracle.rel_err_covs(S, d[f"S_{ref}"]) < TOL
+    check(P, X, S)
+
+
+@pytest.mark.parametrize("k", list(range(1, 18)) + [31, 32, 33, 63, 64, 65, 100, 257])
+def test_lengths_every_parity_pattern(k):
+    P = pb.constant_velocity([k], seed=k)
+    X, S = native.smooth(P)
+    check(P, X, S)
+
+
+@pytest.mark.parametrize("n,m", [(1, 1), (2, 1), (3, 6), (4, 2), (5, 3), (6, 3), (8, 4), (12, 6)])
+@pytest.mark.parametrize("cov", ["C", "W", "w", "F"])
+def test_shapes_cov_types_missing(n, m, cov):
+    """Tall and flat G, every covariance form, 35% missing observations
+    (including the consecutive and trailing ones the reference rejects)."""
+    P = pb.random_dynamics([13, 6, 1, 9, 2], n, m, seed=n * 10 + m, K_type=cov, C_type=cov, missing=0.35,
+                           per_step=True)
+    X, S = native.smooth(P)
+    check(P, X, S)
+    Xd, Sd = oracle.dense_smooth(P)
+    assert oracle.rel_err_states(X, Xd) < TOL
+    assert oracle.rel_err_covs(S, Sd) < TOL
+
+
+def test_batched_uneven_tracks():
+    lens = pb.batched_lengths(300, 1, 600, seed=3)
+    P = pb.constant_velocity(lens, seed=4, missing=0.05)
+    X, S = native.smooth(P)
+    check(P, X, S)
+
+
+def test_full_size_single_track_100k():
+    """The plain single-track workload (n=6, m=3, k=100,000) at full size."""
+    P = pb.constant_velocity([100000], seed=11)
+    X, S = native.smooth(P)
+    check(P, X, S)
+
+
+def test_host_and_device_locations_agree():
+    P = pb.random_dynamics([40, 17], 5, 3, seed=2, per_step=True)
+    Xd, Sd = native.smooth(P, location="device")
+    Xh, Sh = native.smooth(P, location="host")
+    np.testing.assert_array_equal(Xd, Xh)
+    np.testing.assert_array_equal(Sd, Sh)
+
+
+def test_no_covariance_gives_same_states():
+    P = pb.constant_velocity([77, 5], seed=6)
+    X1, S1 = native.smooth(P, covariance=True)
+    X2, S2 = native.smooth(P, covariance=False)
+    assert S2 is None
+    np.testing.assert_array_equal(X1, X2)
+
+
+def test_reference_entry_points_with_step_structs():
+    """kalman_smooth_oddeven on kalman_step_equations_t structs, per track and
+    through the batched entry, equals the packed path."""
+    P = pb.random_dynamics([19, 4, 1], 4, 2, seed=8, per_step=True, missing=0.2, K_type="w", C_type="F")
+    Xp, Sp = native.smooth(P)
+    X1, S1, st1 = native.smooth_equations(P, "oddeven")
+    X2, S2, st2 = native.smooth_equations(P, "oddeven", batched=True)
+    assert st1 == 0 and st2 == 0
+    np.testing.assert_array_equal(X1, Xp)
+    np.testing.assert_array_equal(S1, Sp)
+    np.testing.assert_array_equal(X2, Xp)
+    X3, S3, st3 = native.smooth_equations(P, "oddeven", covariance=False)
+    assert S3 is None and st3 == 0
+    np.testing.assert_array_equal(X3, Xp)
+
+
+def test_unobservable_reports_singular():
+    P = pb.constant_velocity([1, 5], seed=1)
+    P.obs_rows[0] = 3  # one step observed by 3 rows of 6 unknowns
+    with pytest.raises(native.KalmanError) as e:
+        native.smooth(P)
+    assert e.value.status == 4
+
+
+def test_malformed_observation_rows_on_device():
+    P = pb.constant_velocity([6], seed=1)
+    P.obs_rows[2] = P.mmax + 3
+    with pytest.raises(native.KalmanError) as e:
+        native.smooth(P, location="device")
+    assert e.value.status == 1

@@ -1,0 +1,699 @@
+/*
+ * host_api.cpp -- the host side of libukgpu.so.
+ *
+ *  - error state (kalman_gpu_last_status / _last_error);
+ *  - the packed entry points of kalman_gpu.h, which stage host arrays to the
+ *    device and back when the caller passes host memory;
+ *  - the reference API of kalman.h for the parallel smoothers:
+ *      kalman_smooth_oddeven / kalman_smooth_associative  (c/kalman.h:148-149)
+ *    marshal the caller's kalman_step_equations_t array into the packed layout,
+ *    run the CUDA smoother and write state/covariance back into the equations;
+ *      kalman_create_options ... kalman_covariance      (c/kalman.h:117-142)
+ *    keep the semantics of the reference's explicit representation
+ *    (c/kalman_explicit_representation.c:164-267 and c/kalman_base.c:231-460):
+ *    evolve/observe store copies of the equations, smooth runs a smoother over
+ *    the stored steps, estimate/covariance return caller-owned copies or
+ *    NaN-filled matrices.
+ *
+ * Nothing here computes a smoothing step on the CPU: the smoothers run only in
+ * the CUDA kernels of oddeven.cu and associative.cu, and fail with an error
+ * (NaN outputs) when no device is usable.
+ */
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <deque>
+#include <vector>
+
+#include "ukgpu_internal.h"
+
+/* -------------------------------------------------------------------------- */
+/* error state                                                                 */
+/* -------------------------------------------------------------------------- */
+
+static thread_local int tl_status = 0;
+static thread_local char tl_message[512] = "";
+
+extern "C" int ukg_set_error(int status, const char* fmt, ...)
+{
+  tl_status = status;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(tl_message, sizeof(tl_message), fmt, ap);
+  va_end(ap);
+  return status;
+}
+
+extern "C" void ukg_clear_error(void)
+{
+  tl_status = 0;
+  tl_message[0] = 0;
+}
+
+extern "C" int kalman_gpu_last_status(void) { return tl_status; }
+extern "C" const char* kalman_gpu_last_error(void) { return tl_message; }
+extern "C" void kalman_gpu_clear_error(void) { ukg_clear_error(); }
+
+/* -------------------------------------------------------------------------- */
+/* packed problems                                                             */
+/* -------------------------------------------------------------------------- */
+
+extern "C" int ukg_validate_problem(const kalman_gpu_problem_t* p, int need_cov)
+{
+  if (!p) return ukg_set_error(KALMAN_GPU_EINVAL, "problem is NULL");
+  if (p->n < 1) return ukg_set_error(KALMAN_GPU_EINVAL, "state dimension %d < 1", p->n);
+  if (p->mmax < 0) return ukg_set_error(KALMAN_GPU_EINVAL, "mmax %d < 0", p->mmax);
+  if (p->ntracks < 1 || !p->track_start) return ukg_set_error(KALMAN_GPU_EINVAL, "no tracks");
+  if (p->location != KALMAN_GPU_DEVICE && p->location != KALMAN_GPU_HOST)
+    return ukg_set_error(KALMAN_GPU_EINVAL, "unknown array location %d", p->location);
+  if (p->track_start[0] != 0) return ukg_set_error(KALMAN_GPU_EINVAL, "track_start[0] must be 0");
+  for (int t = 0; t < p->ntracks; ++t)
+    if (p->track_start[t + 1] < p->track_start[t])
+      return ukg_set_error(KALMAN_GPU_EINVAL, "track_start is decreasing at track %d", t);
+  if (p->track_start[p->ntracks] != p->nsteps)
+    return ukg_set_error(KALMAN_GPU_EINVAL, "track_start[ntracks] != nsteps");
+  if (p->nsteps > 0) {
+    if (!p->H || !p->F || !p->c || !p->K || !p->K_type || !p->obs_rows || !p->state)
+      return ukg_set_error(KALMAN_GPU_EINVAL, "a required array is NULL");
+    if (p->mmax > 0 && (!p->G || !p->o || !p->C || !p->C_type))
+      return ukg_set_error(KALMAN_GPU_EINVAL, "observation arrays are NULL");
+    if (need_cov && !p->covariance) return ukg_set_error(KALMAN_GPU_EINVAL, "covariance output is NULL");
+  }
+  if (p->location == KALMAN_GPU_HOST && p->nsteps > 0) {
+    for (int64_t s = 0; s < p->nsteps; ++s)
+      if (p->obs_rows[s] < 0 || p->obs_rows[s] > p->mmax)
+        return ukg_set_error(KALMAN_GPU_EINVAL, "obs_rows[%lld] = %d outside [0, %d]", (long long)s,
+                             p->obs_rows[s], p->mmax);
+  }
+  return 0;
+}
+
+namespace {
+
+struct Stage {
+  int device = -1;
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+thread_local Stage tl_stage; /* device copy of host-located packed problems */
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+int device_ready()
+{
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return ukg_set_error(KALMAN_GPU_ENODEV, "no CUDA device is available (%s)",
+                         e == cudaSuccess ? "device count is 0" : cudaGetErrorString(e));
+  }
+  return 0;
+}
+
+typedef int (*device_smoother)(uint32_t, const kalman_gpu_problem_t*, void*);
+
+/* Runs a device smoother on a packed problem held in host memory: copies the
+ * inputs into a cached device buffer, runs, copies the outputs back.         */
+int run_host_problem(device_smoother fn, uint32_t options, const kalman_gpu_problem_t* p, bool want_cov,
+                     cudaStream_t st)
+{
+  const int64_t N = p->nsteps, n = p->n, mm = p->mmax;
+  const size_t sz[] = {
+      (size_t)(N * n * n * 8), (size_t)(N * n * n * 8), (size_t)(N * n * 8), (size_t)(N * n * n * 8), (size_t)N,
+      (size_t)(N * mm * n * 8), (size_t)(N * mm * 8), (size_t)(N * mm * mm * 8), (size_t)N, (size_t)(N * 4),
+      (size_t)(N * n * 8), want_cov ? (size_t)(N * n * n * 8) : 0};
+  const void* src[] = {p->H, p->F, p->c, p->K, p->K_type, p->G, p->o, p->C, p->C_type, p->obs_rows};
+  size_t off[12], total = 0;
+  for (int i = 0; i < 12; ++i) {
+    off[i] = total;
+    total = align_up(total + sz[i], 256);
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  Stage& S = tl_stage;
+  if (S.p && (S.bytes < total || S.device != dev)) {
+    cudaFree(S.p);
+    S = Stage();
+  }
+  if (!S.p) {
+    cudaError_t e = cudaMalloc(&S.p, total);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      S = Stage();
+      return ukg_set_error(KALMAN_GPU_ENOMEM, "cudaMalloc of %zu bytes for the problem failed", total);
+    }
+    S.bytes = total;
+    S.device = dev;
+  }
+  char* D = (char*)S.p;
+  for (int i = 0; i < 10; ++i)
+    if (sz[i] && src[i]) cudaMemcpyAsync(D + off[i], src[i], sz[i], cudaMemcpyHostToDevice, st);
+  kalman_gpu_problem_t d = *p;
+  d.location = KALMAN_GPU_DEVICE;
+  d.H = (const double*)(D + off[0]);
+  d.F = (const double*)(D + off[1]);
+  d.c = (const double*)(D + off[2]);
+  d.K = (const double*)(D + off[3]);
+  d.K_type = (const char*)(D + off[4]);
+  d.G = (const double*)(D + off[5]);
+  d.o = (const double*)(D + off[6]);
+  d.C = (const double*)(D + off[7]);
+  d.C_type = (const char*)(D + off[8]);
+  d.obs_rows = (const int32_t*)(D + off[9]);
+  d.state = (double*)(D + off[10]);
+  d.covariance = want_cov ? (double*)(D + off[11]) : nullptr;
+  int status = fn(options, &d, st);
+  if (status != KALMAN_GPU_ECUDA) {
+    cudaMemcpyAsync(p->state, d.state, sz[10], cudaMemcpyDeviceToHost, st);
+    if (want_cov) cudaMemcpyAsync(p->covariance, d.covariance, sz[11], cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return ukg_set_error(KALMAN_GPU_ECUDA, "copying results back: %s", cudaGetErrorString(e));
+  }
+  return status;
+}
+
+int smooth_packed(device_smoother fn, uint32_t options, const kalman_gpu_problem_t* p, void* stream)
+{
+  ukg_clear_error();
+  const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p && p->covariance;
+  if (int e = ukg_validate_problem(p, 0)) return e;
+  if (p->nsteps == 0) return 0;
+  if (int e = device_ready()) return e;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (p->location == KALMAN_GPU_HOST) return run_host_problem(fn, options, p, want_cov, st);
+  return fn(options, p, st);
+}
+
+}  // namespace
+
+extern "C" int kalman_gpu_smooth_oddeven_packed(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream)
+{
+  return smooth_packed(ukg_oddeven_device, options, p, cuda_stream);
+}
+
+extern "C" int kalman_gpu_smooth_associative_packed(uint32_t options, const kalman_gpu_problem_t* p,
+                                                    void* cuda_stream)
+{
+  return smooth_packed(ukg_associative_device, options, p, cuda_stream);
+}
+
+extern "C" void ukg_release_oddeven_workspace(void);
+extern "C" void ukg_release_associative_workspace(void);
+
+extern "C" void kalman_gpu_release(void)
+{
+  ukg_release_oddeven_workspace();
+  ukg_release_associative_workspace();
+  if (tl_stage.p) cudaFree(tl_stage.p);
+  tl_stage = Stage();
+}
+
+/* -------------------------------------------------------------------------- */
+/* marshalling kalman_step_equations_t arrays                                  */
+/* -------------------------------------------------------------------------- */
+
+namespace {
+
+int rows_of(const kalman_matrix_t* A) { return A ? A->row_dim : 0; }
+int cols_of(const kalman_matrix_t* A) { return A ? A->col_dim : 0; }
+
+void copy_block(double* dst, int ld, const kalman_matrix_t* A)
+{
+  for (int j = 0; j < A->col_dim; ++j)
+    for (int i = 0; i < A->row_dim; ++i) dst[(size_t)j * ld + i] = A->elements[(size_t)j * A->ld + i];
+}
+
+kalman_matrix_t* new_matrix(int rows, int cols)
+{
+  kalman_matrix_t* M = (kalman_matrix_t*)malloc(sizeof(kalman_matrix_t));
+  M->row_dim = rows;
+  M->col_dim = cols;
+  M->ld = rows;
+  M->elements = (rows > 0 && cols > 0) ? (double*)malloc(sizeof(double) * rows * cols) : nullptr;
+  return M;
+}
+
+void free_matrix(kalman_matrix_t* M)
+{
+  if (!M) return;
+  free(M->elements);
+  free(M);
+}
+
+bool valid_cov(const kalman_matrix_t* Cm, char type, int dim)
+{
+  if (!Cm || !Cm->elements) return false;
+  if (type == 'w') return Cm->row_dim == dim && Cm->col_dim >= 1;
+  if (type == 'W' || type == 'C' || type == 'U' || type == 'F') return Cm->row_dim == dim && Cm->col_dim == dim;
+  return false;
+}
+
+/* Host staging of the packed image of an equations array (page-locked when
+ * possible, so the copies to the device run at full speed).                 */
+struct HostPack {
+  std::vector<int64_t> track_start;
+  double *H = nullptr, *F = nullptr, *c = nullptr, *K = nullptr, *G = nullptr, *o = nullptr, *C = nullptr;
+  double *state = nullptr, *cov = nullptr;
+  char *Kt = nullptr, *Ct = nullptr;
+  int32_t* m = nullptr;
+  void* block = nullptr;
+  bool pinned = false;
+  ~HostPack()
+  {
+    if (block) {
+      if (pinned) cudaFreeHost(block);
+      else free(block);
+    }
+  }
+};
+
+int pack_equations(kalman_step_equations_t** eq, int64_t N, const kalman_step_index_t* lengths, int ntracks,
+                   bool want_cov, HostPack& hp, kalman_gpu_problem_t& P)
+{
+  if (!eq) return ukg_set_error(KALMAN_GPU_EINVAL, "equations is NULL");
+  for (int64_t s = 0; s < N; ++s)
+    if (!eq[s]) return ukg_set_error(KALMAN_GPU_EINVAL, "equations[%lld] is NULL", (long long)s);
+  const int n = eq[0]->dimension;
+  if (n < 1) return ukg_set_error(KALMAN_GPU_EINVAL, "state dimension %d < 1", n);
+  hp.track_start.assign(ntracks + 1, 0);
+  for (int t = 0; t < ntracks; ++t) {
+    if (lengths[t] < 0) return ukg_set_error(KALMAN_GPU_EINVAL, "negative track length");
+    hp.track_start[t + 1] = hp.track_start[t] + (int64_t)lengths[t];
+  }
+  if (hp.track_start[ntracks] != N) return ukg_set_error(KALMAN_GPU_EINVAL, "track lengths do not sum to the step count");
+  int mmax = 0;
+  std::vector<char> first(N, 0);
+  for (int t = 0; t < ntracks; ++t)
+    if (lengths[t] > 0) first[hp.track_start[t]] = 1;
+  for (int64_t s = 0; s < N; ++s) {
+    const kalman_step_equations_t* e = eq[s];
+    if (e->dimension != n)
+      return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld has dimension %d, step 0 has %d; steps of different "
+                           "dimensions are not supported", (long long)s, e->dimension, n);
+    if (!first[s]) {
+      if (rows_of(e->H) != n || cols_of(e->H) != n || rows_of(e->F) != n || cols_of(e->F) != n ||
+          rows_of(e->c) != n || cols_of(e->c) != 1 || !e->H->elements || !e->F->elements || !e->c->elements)
+        return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld: H and F must be %dx%d and c %dx1", (long long)s, n, n, n);
+      if (!valid_cov(e->K, e->K_type, n))
+        return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld: bad evolution covariance (type '%c')", (long long)s,
+                             e->K_type ? e->K_type : '?');
+    }
+    if (e->o) {
+      const int m = rows_of(e->o);
+      if (m < 1 || cols_of(e->o) != 1 || rows_of(e->G) != m || cols_of(e->G) != n || !e->G->elements ||
+          !e->o->elements)
+        return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld: G must be m x %d and o m x 1", (long long)s, n);
+      if (!valid_cov(e->C, e->C_type, m))
+        return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld: bad observation covariance (type '%c')", (long long)s,
+                             e->C_type ? e->C_type : '?');
+      if (m > mmax) mmax = m;
+    }
+  }
+  const size_t nn = (size_t)n * n, mm = (size_t)mmax;
+  const size_t dbl = N * (3 * nn + n + mm * n + mm + mm * mm + n + (want_cov ? nn : 0));
+  const size_t bytes = dbl * sizeof(double) + 2 * N + 4 * N + 64;
+  if (cudaHostAlloc(&hp.block, bytes, cudaHostAllocDefault) == cudaSuccess) {
+    hp.pinned = true;
+  } else {
+    cudaGetLastError();
+    hp.block = malloc(bytes);
+    if (!hp.block) return ukg_set_error(KALMAN_GPU_ENOMEM, "host allocation of %zu bytes failed", bytes);
+  }
+  double* d = (double*)hp.block;
+  hp.H = d; d += N * nn;
+  hp.F = d; d += N * nn;
+  hp.K = d; d += N * nn;
+  hp.c = d; d += N * n;
+  hp.G = d; d += N * mm * n;
+  hp.o = d; d += N * mm;
+  hp.C = d; d += N * mm * mm;
+  hp.state = d; d += N * n;
+  hp.cov = want_cov ? d : nullptr; d += want_cov ? N * nn : 0;
+  hp.m = (int32_t*)d;
+  hp.Kt = (char*)(hp.m + N);
+  hp.Ct = hp.Kt + N;
+  memset(hp.block, 0, (char*)(hp.Ct + N) - (char*)hp.block);
+  for (int64_t s = 0; s < N; ++s) {
+    const kalman_step_equations_t* e = eq[s];
+    hp.Kt[s] = 'C';
+    hp.Ct[s] = 'C';
+    if (!first[s]) {
+      copy_block(hp.H + s * nn, n, e->H);
+      copy_block(hp.F + s * nn, n, e->F);
+      copy_block(hp.c + s * n, n, e->c);
+      if (e->K_type == 'w') {
+        for (int i = 0; i < n; ++i) hp.K[s * nn + i] = e->K->elements[i];
+      } else {
+        copy_block(hp.K + s * nn, n, e->K);
+      }
+      hp.Kt[s] = e->K_type;
+    }
+    if (e->o) {
+      const int m = e->o->row_dim;
+      hp.m[s] = m;
+      copy_block(hp.G + s * mm * n, (int)mm, e->G);
+      for (int i = 0; i < m; ++i) hp.o[s * mm + i] = e->o->elements[i];
+      if (e->C_type == 'w') {
+        for (int i = 0; i < m; ++i) hp.C[s * mm * mm + i] = e->C->elements[i];
+      } else {
+        copy_block(hp.C + s * mm * mm, (int)mm, e->C);
+      }
+      hp.Ct[s] = e->C_type;
+    }
+  }
+  memset(&P, 0, sizeof(P));
+  P.n = n;
+  P.mmax = mmax;
+  P.ntracks = ntracks;
+  P.location = KALMAN_GPU_HOST;
+  P.nsteps = N;
+  P.track_start = hp.track_start.data();
+  P.H = hp.H; P.F = hp.F; P.c = hp.c; P.K = hp.K; P.K_type = hp.Kt;
+  P.G = hp.G; P.o = hp.o; P.C = hp.C; P.C_type = hp.Ct; P.obs_rows = hp.m;
+  P.state = hp.state;
+  P.covariance = hp.cov;
+  return 0;
+}
+
+/* writes the results into the equations (caller-owned matrices, type 'C') */
+void unpack_results(kalman_step_equations_t** eq, int64_t N, int n0, const double* state, const double* cov,
+                    bool failed)
+{
+  for (int64_t s = 0; s < N; ++s) {
+    kalman_step_equations_t* e = eq[s];
+    if (!e) continue;
+    const int n = failed ? e->dimension : n0;
+    if (n < 1) continue;
+    const size_t nn = (size_t)n * n;
+    free_matrix(e->state);
+    free_matrix(e->covariance);
+    e->state = new_matrix(n, 1);
+    for (int i = 0; i < n; ++i) e->state->elements[i] = failed ? NAN : state[s * n + i];
+    e->covariance = nullptr;
+    if (cov || failed) {
+      e->covariance = new_matrix(n, n);
+      for (size_t i = 0; i < nn; ++i) e->covariance->elements[i] = failed ? NAN : cov[s * nn + i];
+    }
+    e->covariance_type = 'C';
+  }
+}
+
+int smooth_equations(bool associative, uint32_t options, kalman_step_equations_t** eq, int64_t N,
+                     const kalman_step_index_t* lengths, int ntracks)
+{
+  ukg_clear_error();
+  if (N <= 0) return 0;
+  /* the reference's associative smoother always returns covariances */
+  const bool want_cov = associative || !(options & KALMAN_NO_COVARIANCE);
+  if (associative) options &= ~(uint32_t)KALMAN_NO_COVARIANCE;
+  HostPack hp;
+  kalman_gpu_problem_t P;
+  int status = pack_equations(eq, N, lengths, ntracks, want_cov, hp, P);
+  if (status == 0) status = device_ready();
+  if (status == 0)
+    status = run_host_problem(associative ? ukg_associative_device : ukg_oddeven_device, options, &P, want_cov,
+                              (cudaStream_t)0);
+  const bool values = (status == 0 || status == KALMAN_GPU_ESINGULAR) && hp.block;
+  if (eq) unpack_results(eq, N, values ? P.n : 0, hp.state, want_cov ? hp.cov : nullptr, !values);
+  return status;
+}
+
+}  // namespace
+
+extern "C" void kalman_smooth_oddeven(kalman_options_t options, kalman_step_equations_t** equations,
+                                      kalman_step_index_t length)
+{
+  kalman_step_index_t L = length;
+  smooth_equations(false, (uint32_t)options, equations, (int64_t)length, &L, 1);
+}
+
+extern "C" void kalman_smooth_associative(kalman_options_t options, kalman_step_equations_t** equations,
+                                          kalman_step_index_t length)
+{
+  kalman_step_index_t L = length;
+  smooth_equations(true, (uint32_t)options, equations, (int64_t)length, &L, 1);
+}
+
+extern "C" int kalman_gpu_smooth_tracks(uint32_t options, kalman_step_equations_t** equations,
+                                        const kalman_step_index_t* track_lengths, int32_t ntracks)
+{
+  if (ntracks < 1 || !track_lengths) return ukg_set_error(KALMAN_GPU_EINVAL, "no tracks");
+  int64_t N = 0;
+  for (int t = 0; t < ntracks; ++t) N += track_lengths[t];
+  const bool assoc = (options & KALMAN_ALGORITHM_ASSOCIATIVE) && !(options & KALMAN_ALGORITHM_ODDEVEN);
+  return smooth_equations(assoc, options, equations, N, track_lengths, ntracks);
+}
+
+/* -------------------------------------------------------------------------- */
+/* kalman_t: the explicit representation                                       */
+/* -------------------------------------------------------------------------- */
+
+struct kalman_st {
+  uint32_t options;
+  std::deque<kalman_step_equations_t*> steps; /* steps.front() has logical index `first` */
+  int64_t first;
+  kalman_step_equations_t* current;
+};
+
+namespace {
+
+kalman_matrix_t* copy_or_null(const kalman_matrix_t* A)
+{
+  if (!A) return nullptr;
+  kalman_matrix_t* B = new_matrix(A->row_dim, A->col_dim);
+  for (int j = 0; j < A->col_dim; ++j)
+    for (int i = 0; i < A->row_dim; ++i) B->elements[(size_t)j * B->ld + i] = A->elements[(size_t)j * A->ld + i];
+  return B;
+}
+
+kalman_step_equations_t* step_new()
+{
+  kalman_step_equations_t* s = (kalman_step_equations_t*)calloc(1, sizeof(kalman_step_equations_t));
+  s->step = -1;
+  s->dimension = -1;
+  s->covariance_type = 'C';
+  return s;
+}
+
+void step_release_observation(kalman_step_equations_t* s)
+{
+  free_matrix(s->G); s->G = nullptr;
+  free_matrix(s->o); s->o = nullptr;
+  free_matrix(s->C); s->C = nullptr;
+  free_matrix(s->state); s->state = nullptr;
+  free_matrix(s->covariance); s->covariance = nullptr;
+}
+
+void step_delete(kalman_step_equations_t* s)
+{
+  if (!s) return;
+  step_release_observation(s);
+  free_matrix(s->H);
+  free_matrix(s->F);
+  free_matrix(s->K);
+  free_matrix(s->c);
+  free(s);
+}
+
+kalman_matrix_t* nan_matrix(int rows, int cols)
+{
+  kalman_matrix_t* M = new_matrix(rows, cols);
+  for (int i = 0; i < rows * cols; ++i) M->elements[i] = NAN;
+  return M;
+}
+
+int64_t resolve(kalman_t* k, kalman_step_index_t si)
+{
+  int64_t last = k->first + (int64_t)k->steps.size() - 1;
+  return si < 0 ? last : (int64_t)si;
+}
+
+kalman_step_equations_t* step_at(kalman_t* k, int64_t si)
+{
+  int64_t pos = si - k->first;
+  if (pos < 0 || pos >= (int64_t)k->steps.size()) return nullptr;
+  return k->steps[(size_t)pos];
+}
+
+}  // namespace
+
+extern "C" kalman_t* kalman_create_options(uint32_t options)
+{
+  const uint32_t alg = options & (KALMAN_ALGORITHM_ULTIMATE | KALMAN_ALGORITHM_CONVENTIONAL |
+                                  KALMAN_ALGORITHM_ODDEVEN | KALMAN_ALGORITHM_ASSOCIATIVE);
+  if (alg != KALMAN_ALGORITHM_ODDEVEN && alg != KALMAN_ALGORITHM_ASSOCIATIVE) {
+    ukg_set_error(KALMAN_GPU_EINVAL, "algorithm bits 0x%x: this library provides KALMAN_ALGORITHM_ODDEVEN and "
+                  "KALMAN_ALGORITHM_ASSOCIATIVE only", alg);
+    return nullptr;
+  }
+  kalman_t* k = new kalman_st();
+  k->options = options;
+  k->first = 0;
+  k->current = nullptr;
+  return k;
+}
+
+extern "C" kalman_t* kalman_create(void) { return kalman_create_options(KALMAN_ALGORITHM_ODDEVEN); }
+
+extern "C" void kalman_free(kalman_t* k)
+{
+  if (!k) return;
+  for (auto* s : k->steps) step_delete(s);
+  if (k->current) step_delete(k->current);
+  delete k;
+}
+
+extern "C" kalman_step_index_t kalman_earliest(kalman_t* k)
+{
+  if (!k || k->steps.empty()) return -1;
+  return (kalman_step_index_t)k->steps.front()->step;
+}
+
+extern "C" kalman_step_index_t kalman_latest(kalman_t* k)
+{
+  if (!k || k->steps.empty()) return -1;
+  return (kalman_step_index_t)k->steps.back()->step;
+}
+
+extern "C" void kalman_evolve(kalman_t* k, int32_t n_i, kalman_matrix_t* H_i, kalman_matrix_t* F_i,
+                              kalman_matrix_t* c_i, kalman_matrix_t* K_i, char K_type)
+{
+  if (!k) return;
+  if (k->current) step_delete(k->current);
+  kalman_step_equations_t* s = step_new();
+  k->current = s;
+  s->dimension = n_i;
+  if (k->steps.empty()) {
+    s->step = 0;
+    return;
+  }
+  s->step = k->steps.back()->step + 1;
+  s->H = copy_or_null(H_i);
+  s->F = copy_or_null(F_i);
+  s->c = copy_or_null(c_i);
+  s->K = copy_or_null(K_i);
+  s->K_type = K_type;
+}
+
+extern "C" void kalman_observe(kalman_t* k, kalman_matrix_t* G_i, kalman_matrix_t* o_i, kalman_matrix_t* C_i,
+                               char C_type)
+{
+  if (!k || !k->current) {
+    ukg_set_error(KALMAN_GPU_EINVAL, "kalman_observe without a preceding kalman_evolve");
+    return;
+  }
+  kalman_step_equations_t* s = k->current;
+  if (o_i) {
+    s->G = copy_or_null(G_i);
+    s->o = copy_or_null(o_i);
+    s->C = copy_or_null(C_i);
+    s->C_type = C_type;
+  }
+  if (k->steps.empty()) k->first = s->step;
+  k->steps.push_back(s);
+  k->current = nullptr;
+}
+
+extern "C" void kalman_smooth(kalman_t* k)
+{
+  if (!k || k->steps.empty()) return;
+  std::vector<kalman_step_equations_t*> v(k->steps.begin(), k->steps.end());
+  if (k->options & KALMAN_ALGORITHM_ODDEVEN)
+    kalman_smooth_oddeven((kalman_options_t)k->options, v.data(), (kalman_step_index_t)v.size());
+  if (k->options & KALMAN_ALGORITHM_ASSOCIATIVE)
+    kalman_smooth_associative((kalman_options_t)k->options, v.data(), (kalman_step_index_t)v.size());
+}
+
+extern "C" kalman_matrix_t* kalman_estimate(kalman_t* k, kalman_step_index_t si)
+{
+  if (!k || k->steps.empty()) return nullptr;
+  kalman_step_equations_t* s = step_at(k, resolve(k, si));
+  if (!s) return nullptr;
+  if (!s->state) return nan_matrix(s->dimension, 1);
+  return copy_or_null(s->state);
+}
+
+extern "C" kalman_matrix_t* kalman_covariance(kalman_t* k, kalman_step_index_t si)
+{
+  if (!k || k->steps.empty()) return nullptr;
+  kalman_step_equations_t* s = step_at(k, resolve(k, si));
+  if (!s) return nullptr;
+  if (!s->covariance) return nan_matrix(s->dimension, s->dimension);
+  return copy_or_null(s->covariance);
+}
+
+extern "C" char kalman_covariance_type(kalman_t* k, kalman_step_index_t si)
+{
+  if (!k || k->steps.empty()) return '-';
+  kalman_step_equations_t* s = step_at(k, resolve(k, si));
+  return s ? s->covariance_type : '-';
+}
+
+extern "C" void kalman_forget(kalman_t* k, kalman_step_index_t si)
+{
+  if (!k || k->steps.empty()) return;
+  const int64_t last = k->first + (int64_t)k->steps.size() - 1;
+  int64_t upto = si < 0 ? last - 1 : (int64_t)si;
+  if (upto > last - 1) return; /* the last step is never forgotten */
+  if (upto < k->first) return;
+  while (k->first <= upto) {
+    step_delete(k->steps.front());
+    k->steps.pop_front();
+    ++k->first;
+  }
+}
+
+extern "C" void kalman_rollback(kalman_t* k, kalman_step_index_t si)
+{
+  if (!k || k->steps.empty()) return;
+  const int64_t last = k->first + (int64_t)k->steps.size() - 1;
+  if (si > last || si < k->first) return;
+  while (!k->steps.empty()) {
+    kalman_step_equations_t* s = k->steps.back();
+    k->steps.pop_back();
+    if (s->step == si) {
+      step_release_observation(s); /* back to "just after evolve" */
+      if (k->current) step_delete(k->current);
+      k->current = s;
+      break;
+    }
+    step_delete(s);
+  }
+}
+
+extern "C" kalman_matrix_t* kalman_perftest(kalman_t* k, kalman_matrix_t* H, kalman_matrix_t* F, kalman_matrix_t* c,
+                                            kalman_matrix_t* K, char K_type, kalman_matrix_t* G, kalman_matrix_t* o,
+                                            kalman_matrix_t* C, char C_type, int32_t count, int32_t decimation)
+{
+  /* the reference's sequential-filter timing loop (c/kalman_base.c:464-512):
+     evolve, observe, estimate, forget, averaging wall time per decimation block */
+  if (decimation < 1) decimation = 1;
+  kalman_matrix_t* t = nan_matrix(count / decimation, 1);
+  const int n = cols_of(G);
+  struct timespec b, e;
+  clock_gettime(CLOCK_MONOTONIC, &b);
+  int j = 0;
+  for (int i = 0; i < count; ++i) {
+    kalman_evolve(k, n, H, F, c, K, K_type);
+    kalman_observe(k, G, o, C, C_type);
+    free_matrix(kalman_estimate(k, -1));
+    kalman_forget(k, -1);
+    if ((i % decimation) == decimation - 1 && j < count / decimation) {
+      clock_gettime(CLOCK_MONOTONIC, &e);
+      t->elements[j++] = ((e.tv_sec - b.tv_sec) + 1e-9 * (e.tv_nsec - b.tv_nsec)) / decimation;
+      b = e;
+    }
+  }
+  return t;
+}
+
+/* the reference's thread controls (c/parallel.h:31-32): the GPU build sizes its
+   launches itself, so these are accepted and ignored                          */
+extern "C" void parallel_set_thread_limit(int number_of_threads) { (void)number_of_threads; }
+extern "C" void parallel_set_blocksize(int blocksize_in) { (void)blocksize_in; }

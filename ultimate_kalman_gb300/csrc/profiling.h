@@ -1,0 +1,34 @@
+/* profiling.h -- internal hooks of profiling.cu (per-kernel CUDA-event timing) */
+#ifndef UKGPU_PROFILING_H
+#define UKGPU_PROFILING_H
+
+#include <cuda_runtime.h>
+
+enum {
+  UKG_K_WEIGH = 0,
+  UKG_K_PAIR,
+  UKG_K_TAIL,
+  UKG_K_SOLVE,
+  UKG_K_AS_ELEMENT,
+  UKG_K_AS_SCAN,
+  UKG_K_AS_SMOOTH,
+  UKG_K_REFINE,
+  UKG_K_PAIR32,
+  UKG_K_SOLVE32,
+  UKG_K_COUNT
+};
+
+void ukg_prof_before(cudaStream_t st, int kind, cudaEvent_t* mark);
+void ukg_prof_after(cudaStream_t st, int kind, cudaEvent_t mark);
+void ukg_prof_collect(void);
+
+/* brackets one kernel launch statement */
+#define UKG_LAUNCH(kind, stream, launch)              \
+  do {                                                \
+    cudaEvent_t ukg_mark_ = nullptr;                  \
+    ukg_prof_before((stream), (kind), &ukg_mark_);    \
+    launch;                                           \
+    ukg_prof_after((stream), (kind), ukg_mark_);      \
+  } while (0)
+
+#endif

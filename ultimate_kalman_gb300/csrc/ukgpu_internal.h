@@ -1,0 +1,34 @@
+/*
+ * ukgpu_internal.h -- declarations shared by the translation units of
+ * libukgpu.so (not installed; clients include include/kalman.h and
+ * include/kalman_gpu.h).
+ */
+#ifndef UKGPU_INTERNAL_H
+#define UKGPU_INTERNAL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "kalman_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* thread-local last error (host_api.cpp) */
+int  ukg_set_error(int status, const char* fmt, ...);
+void ukg_clear_error(void);
+
+/* device smoothers on a packed problem whose arrays are in device memory
+ * (oddeven.cu / associative.cu); cuda_stream may be NULL                      */
+int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream);
+int ukg_associative_device(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream);
+
+/* checks the arguments of a packed problem that do not need device access   */
+int ukg_validate_problem(const kalman_gpu_problem_t* p, int need_cov);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

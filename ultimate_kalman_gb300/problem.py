@@ -97,7 +97,9 @@ def constant_velocity(lengths, seed=0, K_type="C", C_type="C", missing=0.0, fold
     H=I, process noise cov diag(1e-2), observation G=[I 0] (m=3) with noise cov
     diag(1e-1), initial state N(0, I).  With fold=True the prior and the first
     measurement become a square 6x6 step-0 observation with identity 'W'
-    weights (the form all three reference smoothers accept)."""
+    weights (the form all three reference smoothers accept).  Every step
+    carries its own copy of the matrices, as the reference's evolve/observe
+    store them."""
     rng = np.random.default_rng(seed)
     lengths = np.asarray(lengths, dtype=np.int64)
     n, m, dt = 6, 3, 0.1
@@ -107,37 +109,43 @@ def constant_velocity(lengths, seed=0, K_type="C", C_type="C", missing=0.0, fold
     G[:, :3] = np.eye(3)
     q, r = 1e-2, 1e-1
     P = empty_problem(n, n, lengths)
+    N = P.nsteps
     T = len(lengths)
-    kmax = int(lengths.max())
+    ts = P.track_start
+    firsts = ts[:-1][lengths > 0]
+    P.H[:] = np.eye(n)
+    P.F[:] = F.T
+    allsteps = np.arange(N)
+    _set_cov(P.K, P.K_type, allsteps, n, q * np.eye(n), K_type)
+    P.G[:, :, :m] = G.T
+    _set_cov(P.C, P.C_type, allsteps, m, r * np.eye(m), C_type)
+    P.obs_rows[:] = m
+    # trajectories and observations, vectorised over tracks
+    kmax = int(lengths.max()) if T else 0
     x = rng.standard_normal((T, n))
+    Y = np.zeros((N, m))
     for i in range(kmax):
-        alive = lengths > i
-        tr = np.nonzero(alive)[0]
-        s = P.track_start[tr] + i
+        tr = np.nonzero(lengths > i)[0]
         if i > 0:
             x[tr] = x[tr] @ F.T + np.sqrt(q) * rng.standard_normal((len(tr), n))
-        y = x[tr] @ G.T + np.sqrt(r) * rng.standard_normal((len(tr), m))
-        P.H[s] = np.eye(n)
-        P.F[s] = F.T
-        _set_cov(P.K, P.K_type, s, n, q * np.eye(n), K_type)
-        if i == 0 and fold:
-            Wobs = np.eye(m) / np.sqrt(r)
-            for a, (tt, ss) in enumerate(zip(tr, s)):
-                R0, o0 = _fold_prior(G, y[a], Wobs, np.zeros(n), np.eye(n))
-                P.G[ss, :, :n] = R0.T
-                P.o[ss, :n] = o0
-                P.C[ss, :n, :n] = np.eye(n)
-                P.C_type[ss] = ord("W")
-                P.obs_rows[ss] = n
-            continue
-        obs = np.ones(len(tr), dtype=bool)
-        if missing > 0 and i > 0:
-            obs = rng.random(len(tr)) >= missing
-        so = s[obs]
-        P.G[so, :, :m] = G.T
-        P.o[so, :m] = y[obs]
-        _set_cov(P.C, P.C_type, so, m, r * np.eye(m), C_type)
-        P.obs_rows[so] = m
+        Y[ts[tr] + i] = x[tr] @ G.T + np.sqrt(r) * rng.standard_normal((len(tr), m))
+    P.o[:, :m] = Y
+    if missing > 0:
+        drop = rng.random(N) < missing
+        drop[firsts] = False
+        P.obs_rows[drop] = 0
+    if fold:
+        Wobs = np.eye(m) / np.sqrt(r)
+        for s in firsts:
+            R0, o0 = _fold_prior(G, Y[s], Wobs, np.zeros(n), np.eye(n))
+            P.G[s] = 0.0
+            P.G[s, :, :n] = R0.T
+            P.o[s] = 0.0
+            P.o[s, :n] = o0
+            P.C[s] = 0.0
+            P.C[s, :n, :n] = np.eye(n)
+            P.C_type[s] = ord("W")
+            P.obs_rows[s] = n
     return P
 
 
