@@ -1,16 +1,1034 @@
 /*
- * associative.cu -- the associative-scan (Sarkka-Garcia-Fernandez) smoother on
- * the GPU.  (Kernels follow in the next commit; until then the entry point
- * reports that it is unavailable.)
+ * associative.cu -- the associative-scan (Sarkka-Garcia-Fernandez) parallel
+ * Kalman smoother on the GPU, FP64.  Restates, as CUDA kernels,
+ * c/kalman_associative_smoother.c of UltimateKalman 2.1.0:
+ *
+ *   element_kernel   build_filtering_element_new 309-505: per step i >= 1 the
+ *                    filtering element (A, b, Z, e, J); step 0 is folded into
+ *                    element 1 through m0 = R^{-1} Q^T (W o_0), P0 = (R^T R)^{-1}
+ *   up/down kernels  prefix_sums_pointers (c/parallel_tbb.cpp:78-121) with
+ *                    filteringAssociativeOperation 889-980 (forward) and
+ *                    smoothingAssociativeOperation 982-1016 (reverse): a
+ *                    work-efficient tree over every track at once -- the
+ *                    up-sweep combines pairs into a half-length level, the
+ *                    down-sweep turns each level into inclusive prefixes in
+ *                    place (about 2 combines per element, depth 2 log2 k)
+ *   smooth_element_kernel  build_smoothing_element_new 697-753
+ *   outputs          filtered_to_state_new / smoothed_to_state_new 1054-1091
+ *
+ * Like the reference, the smoother ignores H (the identity is assumed) and
+ * needs a square weighted G at step 0.  Deviations (also in the oracle): the
+ * last step gets the filtered covariance Z (the reference copies an unset field,
+ * c/kalman_associative_smoother.c:1221, and returns NaN); unobserved steps get
+ * e = 0, J = 0 (the reference dereferences NULL); an unobserved step 1 gets
+ * b = F m0 + c (the reference computes m0 + c).
+ *
+ * One thread per item; its n x n temporaries live in shared memory,
+ * interleaved across the block's threads (element e of thread t at
+ * smem[e*blockDim + t]).  Element arrays are element-major (SoA) so that
+ * consecutive threads touch consecutive addresses.
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "profiling.h"
 #include "ukgpu_internal.h"
 
-extern "C" void ukg_release_associative_workspace(void) {}
+namespace {
+
+struct PV {
+  double* p;
+  int s;
+  __device__ __forceinline__ double& operator[](int i) const { return p[i * s]; }
+  __device__ __forceinline__ PV operator+(int off) const { return PV{p + off * s, s}; }
+};
+
+struct Soa {
+  double* p;
+  int64_t stride;
+  __device__ __forceinline__ double& at(int e, int64_t s) const { return p[(int64_t)e * stride + s]; }
+};
+
+__device__ void householder(PV W, int ld, int rows, int npiv, int cols)
+{
+  const int nref = rows < npiv ? rows : npiv;
+  for (int k = 0; k < nref; ++k) {
+    PV v = W + k * ld;
+    const double alpha = v[k];
+    double tail = 0.0;
+    for (int i = k + 1; i < rows; ++i) tail = fma(v[i], v[i], tail);
+    if (tail == 0.0) continue;
+    const double beta = -copysign(sqrt(fma(alpha, alpha, tail)), alpha);
+    const double t = (beta - alpha) / beta;
+    const double scale = 1.0 / (alpha - beta);
+    for (int i = k + 1; i < rows; ++i) v[i] *= scale;
+    v[k] = beta;
+    for (int j = k + 1; j < cols; ++j) {
+      PV a = W + j * ld;
+      double d = a[k];
+      for (int i = k + 1; i < rows; ++i) d = fma(v[i], a[i], d);
+      d *= t;
+      a[k] -= d;
+      for (int i = k + 1; i < rows; ++i) a[i] = fma(-d, v[i], a[i]);
+    }
+  }
+}
+
+/* W = [A | B] (n x (n+p), ld n): on return W[:, n:n+p] = A^{-1} B (the
+ * reference's QR-based mldivide, c/matrix_ops.c:610-630).  Returns true on a
+ * zero pivot.                                                               */
+__device__ bool solve_square(PV W, int n, int p)
+{
+  householder(W, n, n, n, n + p);
+  bool bad = false;
+  for (int c = 0; c < p; ++c) {
+    PV x = W + (n + c) * n;
+    for (int j = n - 1; j >= 0; --j) {
+      const double d = W[j * n + j];
+      bad |= (d == 0.0);
+      const double xj = x[j] / d;
+      x[j] = xj;
+      for (int i = 0; i < j; ++i) x[i] = fma(-xj, W[j * n + i], x[i]);
+    }
+  }
+  return bad;
+}
+
+/* explicit covariance of a factor (kalman_covariance_matrix_explicit,
+ * c/kalman_base.c:178-214) into out (dim x dim, ld dim); ws: 2*dim*dim      */
+__device__ bool explicit_cov(char type, const double* cov, int ldc, int dim, PV out, PV ws)
+{
+  if (type == 'C') {
+    for (int j = 0; j < dim; ++j)
+      for (int i = 0; i < dim; ++i) out[j * dim + i] = cov[(int64_t)j * ldc + i];
+    return false;
+  }
+  if (type == 'w') {
+    for (int j = 0; j < dim; ++j)
+      for (int i = 0; i < dim; ++i) out[j * dim + i] = (i == j) ? 1.0 / (cov[i] * cov[i]) : 0.0;
+    return false;
+  }
+  if (type == 'U' || type == 'F') { /* L L^T */
+    for (int j = 0; j < dim; ++j)
+      for (int i = 0; i < dim; ++i) {
+        double s = 0.0;
+        for (int k = 0; k < dim; ++k) s = fma(cov[(int64_t)k * ldc + i], cov[(int64_t)k * ldc + j], s);
+        out[j * dim + i] = s;
+      }
+    return false;
+  }
+  if (type == 'W') { /* (W^T W)^{-1} = W^{-1} W^{-T} */
+    for (int j = 0; j < dim; ++j)
+      for (int i = 0; i < dim; ++i) {
+        ws[j * dim + i] = cov[(int64_t)j * ldc + i];
+        ws[(dim + j) * dim + i] = (i == j) ? 1.0 : 0.0;
+      }
+    bool bad = solve_square(ws, dim, dim); /* ws[:, dim:2dim] = W^{-1} */
+    PV Wi = ws + dim * dim;
+    for (int j = 0; j < dim; ++j)
+      for (int i = 0; i < dim; ++i) {
+        double s = 0.0;
+        for (int k = 0; k < dim; ++k) s = fma(Wi[k * dim + i], Wi[k * dim + j], s);
+        out[j * dim + i] = s;
+      }
+    return bad;
+  }
+  return true;
+}
+
+__device__ __forceinline__ bool valid_type(char c)
+{
+  return c == 'W' || c == 'w' || c == 'C' || c == 'U' || c == 'F';
+}
+
+/* weighs column col (rows) by the factor: 'W' W col, 'w' diag, 'C' chol^{-1},
+ * 'U'/'F' tril^{-1}; L: rows x rows scratch                                  */
+__device__ bool weigh_column(char type, const double* cov, int ldc, int rows, PV col, PV L, PV tmp)
+{
+  if (type == 'W') {
+    for (int i = 0; i < rows; ++i) {
+      double s = 0.0;
+      for (int j = 0; j < rows; ++j) s = fma(cov[(int64_t)j * ldc + i], col[j], s);
+      tmp[i] = s;
+    }
+    for (int i = 0; i < rows; ++i) col[i] = tmp[i];
+    return false;
+  }
+  if (type == 'w') {
+    for (int i = 0; i < rows; ++i) col[i] *= cov[i];
+    return false;
+  }
+  bool bad = false;
+  if (type == 'C') {
+    for (int j = 0; j < rows; ++j) {
+      double d = cov[(int64_t)j * ldc + j];
+      for (int k = 0; k < j; ++k) d = fma(-L[k * rows + j], L[k * rows + j], d);
+      if (!(d > 0.0)) bad = true;
+      d = sqrt(d);
+      L[j * rows + j] = d;
+      for (int i = j + 1; i < rows; ++i) {
+        double s = cov[(int64_t)j * ldc + i];
+        for (int k = 0; k < j; ++k) s = fma(-L[k * rows + i], L[k * rows + j], s);
+        L[j * rows + i] = s / d;
+      }
+    }
+  } else {
+    for (int j = 0; j < rows; ++j)
+      for (int i = j; i < rows; ++i) L[j * rows + i] = cov[(int64_t)j * ldc + i];
+  }
+  for (int j = 0; j < rows; ++j) {
+    const double xj = col[j] / L[j * rows + j];
+    col[j] = xj;
+    for (int i = j + 1; i < rows; ++i) col[i] = fma(-xj, L[j * rows + i], col[i]);
+  }
+  return bad;
+}
+
+struct Raw {
+  const double *F, *c, *K, *G, *o, *C;
+  const char *K_type, *C_type;
+  const int32_t* obs_rows;
+  int mmax;
+};
+
+/* filtering elements (A, b, Z, e, J) and smoothing elements (E, g, L) */
+struct FElems {
+  Soa A, b, Z, e, J;
+};
+struct SElems {
+  Soa E, g, L;
+};
+
+struct Args {
+  int n, ntracks;
+  const int64_t* track_start; /* device [T+1] */
+  double* state;              /* filtered, then smoothed, [N][n]   */
+  double* cov;                /* [N][n*n]                           */
+  int* flag;
+};
+
+__device__ __forceinline__ int find_track(const int64_t* base, int T, int64_t i)
+{
+  int lo = 0, hi = T;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (base[mid] <= i) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+/* m0 and P0 from the square weighted step-0 observation; ws: n*(n+1) + 2n*n + n */
+__device__ bool step0_estimate(const Raw& raw, int n, int64_t g0, PV m0, PV P0, PV ws, int* flag)
+{
+  const int mm = raw.mmax, m = raw.obs_rows[g0];
+  if (m != n) {
+    atomicOr(flag, 4);
+    return true;
+  }
+  const char ct = raw.C_type[g0];
+  if (!valid_type(ct)) atomicOr(flag, 4);
+  PV W = ws, L = ws + n * (n + 1), tmp = L + n * n;
+  const double* C = raw.C + g0 * (int64_t)mm * mm;
+  bool bad = false;
+  for (int q = 0; q <= n; ++q) {
+    PV col = W + q * n;
+    for (int i = 0; i < n; ++i) col[i] = q < n ? raw.G[g0 * (int64_t)mm * n + (int64_t)q * mm + i] : raw.o[g0 * mm + i];
+    bad |= weigh_column(ct, C, mm, n, col, L, tmp);
+  }
+  householder(W, n, n, n, n + 1);
+  /* m0 = R^{-1} (Q^T W o) */
+  for (int i = 0; i < n; ++i) m0[i] = W[n * n + i];
+  for (int j = n - 1; j >= 0; --j) {
+    const double d = W[j * n + j];
+    bad |= (d == 0.0);
+    const double xj = m0[j] / d;
+    m0[j] = xj;
+    for (int i = 0; i < j; ++i) m0[i] = fma(-xj, W[j * n + i], m0[i]);
+  }
+  /* P0 = R^{-1} R^{-T}: Ri = R^{-1} column by column into L */
+  for (int q = 0; q < n; ++q) {
+    for (int i = 0; i < n; ++i) L[q * n + i] = (i == q) ? 1.0 : 0.0;
+    for (int j = n - 1; j >= 0; --j) {
+      const double xj = L[q * n + j] / W[j * n + j];
+      L[q * n + j] = xj;
+      for (int i = 0; i < j; ++i) L[q * n + i] = fma(-xj, W[j * n + i], L[q * n + i]);
+    }
+  }
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      double s = 0.0;
+      for (int k = (i > j ? i : j); k < n; ++k) s = fma(L[k * n + i], L[k * n + j], s);
+      P0[j * n + i] = s;
+    }
+  return bad;
+}
+
+/* ---------------------------------------------------------------------------
+ * filtering elements; thread per global step.  Step i of a track writes
+ * element r = i - 1 of the track's level-0 sequence (elements 1..k-1); the
+ * thread of step 0 writes the filtered estimate of step 0.
+ * ------------------------------------------------------------------------ */
+__global__ void element_kernel(Args a, Raw raw, FElems out, const int64_t* seq_start, int64_t nsteps, int mx)
+{
+  extern __shared__ double smem[];
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nsteps) return;
+  const int n = a.n, mm = raw.mmax;
+  const int64_t nn = (int64_t)n * n;
+  const int t = find_track(a.track_start, a.ntracks, g);
+  const int64_t g0 = a.track_start[t], i = g - g0;
+  PV ws{smem + threadIdx.x, (int)blockDim.x};
+  /* layout: m0 (n) | P0 (nn) | Kx (nn) | scratch (rest) */
+  PV m0 = ws, P0 = ws + n, Kx = P0 + n * n, sc = Kx + n * n;
+  bool bad = false;
+  if (i <= 1) {
+    bad |= step0_estimate(raw, n, g0, m0, P0, sc, a.flag);
+    if (i == 0) {
+      for (int r = 0; r < n; ++r) a.state[g0 * n + r] = m0[r];
+      for (int e = 0; e < n * n; ++e) a.cov[g0 * nn + e] = P0[e];
+      if (bad) atomicOr(a.flag, 2);
+      return;
+    }
+  }
+  const int64_t r = seq_start[t] + (i - 1);
+  const double* F = raw.F + g * nn;
+  const double* c = raw.c + g * n;
+  const char kt = raw.K_type[g];
+  if (!valid_type(kt)) atomicOr(a.flag, 4);
+  bad |= explicit_cov(kt, raw.K + g * nn, n, n, Kx, sc);
+  if (i == 1) { /* K_1 += F P0 F^T */
+    PV T = sc; /* F P0 */
+    for (int q = 0; q < n; ++q)
+      for (int p = 0; p < n; ++p) {
+        double s = 0.0;
+        for (int k = 0; k < n; ++k) s = fma(F[k * n + p], P0[q * n + k], s);
+        T[q * n + p] = s;
+      }
+    for (int q = 0; q < n; ++q)
+      for (int p = 0; p < n; ++p) {
+        double s = Kx[q * n + p];
+        for (int k = 0; k < n; ++k) s = fma(T[k * n + p], F[k * n + q], s);
+        Kx[q * n + p] = s;
+      }
+  }
+  int m = raw.obs_rows[g];
+  if (m < 0 || m > mm) {
+    m = 0;
+    atomicOr(a.flag, 4);
+  }
+  if (m == 0) {
+    for (int q = 0; q < n; ++q)
+      for (int p = 0; p < n; ++p) {
+        out.Z.at(q * n + p, r) = Kx[q * n + p];
+        out.A.at(q * n + p, r) = (i == 1) ? 0.0 : F[q * n + p];
+        out.J.at(q * n + p, r) = 0.0;
+      }
+    for (int p = 0; p < n; ++p) {
+      double bp = c[p];
+      if (i == 1)
+        for (int k = 0; k < n; ++k) bp = fma(F[k * n + p], m0[k], bp);
+      out.b.at(p, r) = bp;
+      out.e.at(p, r) = 0.0;
+    }
+    if (bad) atomicOr(a.flag, 2);
+    return;
+  }
+  const double* G = raw.G + g * (int64_t)mm * n;
+  const double* o = raw.o + g * mm;
+  const char ct = raw.C_type[g];
+  if (!valid_type(ct)) atomicOr(a.flag, 4);
+  /* scratch layout: S (m*m) | W = [S^T | G] (m*(m+n)) | GtS (n*m) | Kg (n*m) |
+     res (m) | v (n) | T (n*n) | cov ws (2*m*m)                               */
+  PV S = sc, W = S + m * m, GtS = W + m * (m + n), Kg = GtS + n * m, res = Kg + n * m, v = res + mx, T = v + n,
+     cw = T + n * n;
+  bad |= explicit_cov(ct, raw.C + g * (int64_t)mm * mm, mm, m, S, cw); /* S = C */
+  /* S += G K G^T */
+  for (int q = 0; q < m; ++q)
+    for (int p = 0; p < m; ++p) {
+      double s = S[q * m + p];
+      for (int k = 0; k < n; ++k) {
+        double kg = 0.0; /* (K G^T)[k, q] */
+        for (int l = 0; l < n; ++l) kg = fma(Kx[l * n + k], G[(int64_t)l * mm + q], kg);
+        s = fma(G[(int64_t)k * mm + p], kg, s);
+      }
+      S[q * m + p] = s;
+    }
+  /* G^T S^{-1} = (S^{-T} G)^T: solve S^T X = G */
+  for (int q = 0; q < m; ++q)
+    for (int p = 0; p < m; ++p) W[q * m + p] = S[p * m + q];
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < m; ++p) W[(m + q) * m + p] = G[(int64_t)q * mm + p];
+  bad |= solve_square(W, m, n);
+  for (int q = 0; q < m; ++q)
+    for (int p = 0; p < n; ++p) GtS[q * n + p] = W[(m + p) * m + q];
+  /* gain Kg = Kx GtS (n x m) */
+  for (int q = 0; q < m; ++q)
+    for (int p = 0; p < n; ++p) {
+      double s = 0.0;
+      for (int k = 0; k < n; ++k) s = fma(Kx[k * n + p], GtS[q * n + k], s);
+      Kg[q * n + p] = s;
+    }
+  /* residual against c: res = o - G c */
+  for (int p = 0; p < m; ++p) {
+    double s = o[p];
+    for (int k = 0; k < n; ++k) s = fma(-G[(int64_t)k * mm + p], c[k], s);
+    res[p] = s;
+  }
+  if (i == 1) {
+    /* m1 = F m0 + c, b = m1 + Kg (o - G m1), Z = Kx - Kg S Kg^T, A = 0 */
+    for (int p = 0; p < n; ++p) {
+      double s = c[p];
+      for (int k = 0; k < n; ++k) s = fma(F[k * n + p], m0[k], s);
+      v[p] = s;
+    }
+    for (int p = 0; p < m; ++p) {
+      double s = o[p];
+      for (int k = 0; k < n; ++k) s = fma(-G[(int64_t)k * mm + p], v[k], s);
+      T[p] = s; /* o - G m1 (T as a vector) */
+    }
+    for (int p = 0; p < n; ++p) {
+      double s = v[p];
+      for (int k = 0; k < m; ++k) s = fma(Kg[k * n + p], T[k], s);
+      out.b.at(p, r) = s;
+    }
+    for (int q = 0; q < n; ++q)
+      for (int p = 0; p < n; ++p) {
+        double s = Kx[q * n + p];
+        for (int k = 0; k < m; ++k) {
+          double ks = 0.0; /* (Kg S)[p, k] */
+          for (int l = 0; l < m; ++l) ks = fma(Kg[l * n + p], S[k * m + l], ks);
+          s = fma(-ks, Kg[k * n + q], s);
+        }
+        out.Z.at(q * n + p, r) = s;
+        out.A.at(q * n + p, r) = 0.0;
+      }
+  } else {
+    /* A = F - Kg (G F), b = c + Kg res, Z = Kx - Kg (G Kx) */
+    for (int p = 0; p < n; ++p) {
+      double s = c[p];
+      for (int k = 0; k < m; ++k) s = fma(Kg[k * n + p], res[k], s);
+      out.b.at(p, r) = s;
+    }
+    for (int q = 0; q < n; ++q) {
+      for (int k = 0; k < m; ++k) { /* column q of G F and G Kx into T[0:m], T[m:2m] */
+        double s1 = 0.0, s2 = 0.0;
+        for (int l = 0; l < n; ++l) {
+          s1 = fma(G[(int64_t)l * mm + k], F[q * n + l], s1);
+          s2 = fma(G[(int64_t)l * mm + k], Kx[q * n + l], s2);
+        }
+        T[k] = s1;
+        T[m + k] = s2;
+      }
+      for (int p = 0; p < n; ++p) {
+        double sa = F[q * n + p], sz = Kx[q * n + p];
+        for (int k = 0; k < m; ++k) {
+          sa = fma(-Kg[k * n + p], T[k], sa);
+          sz = fma(-Kg[k * n + p], T[m + k], sz);
+        }
+        out.A.at(q * n + p, r) = sa;
+        out.Z.at(q * n + p, r) = sz;
+      }
+    }
+  }
+  /* e = F^T GtS res, J = F^T GtS G F */
+  for (int p = 0; p < n; ++p) {
+    double s = 0.0;
+    for (int k = 0; k < m; ++k) s = fma(GtS[k * n + p], res[k], s);
+    v[p] = s; /* GtS res */
+  }
+  for (int p = 0; p < n; ++p) {
+    double s = 0.0;
+    for (int k = 0; k < n; ++k) s = fma(F[p * n + k], v[k], s);
+    out.e.at(p, r) = s;
+  }
+  for (int q = 0; q < n; ++q) {
+    for (int k = 0; k < m; ++k) { /* column q of G F */
+      double s1 = 0.0;
+      for (int l = 0; l < n; ++l) s1 = fma(G[(int64_t)l * mm + k], F[q * n + l], s1);
+      T[k] = s1;
+    }
+    for (int p = 0; p < n; ++p) { /* (GtS G F)[:, q] into v */
+      double s = 0.0;
+      for (int k = 0; k < m; ++k) s = fma(GtS[k * n + p], T[k], s);
+      v[p] = s;
+    }
+    for (int p = 0; p < n; ++p) {
+      double s = 0.0;
+      for (int k = 0; k < n; ++k) s = fma(F[p * n + k], v[k], s);
+      out.J.at(q * n + p, r) = s;
+    }
+  }
+  if (bad) atomicOr(a.flag, 2);
+}
+
+/* ---------------------------------------------------------------------------
+ * the two associative operations.  `out` may alias `sj` (never `si`): every
+ * entry of sj is read before the entry of out at the same place is written.
+ * ------------------------------------------------------------------------ */
+__device__ bool combine_filter(int n, const FElems& Xi, int64_t i, const FElems& Xj, int64_t j, const FElems& O,
+                               int64_t o, PV ws)
+{
+  /* ws: W (2n*n) | Xm (n*n) | Ym (n*n) | T (n*n) | v (n) */
+  PV W = ws, Xm = ws + 2 * n * n, Ym = Xm + n * n, T = Ym + n * n, v = T + n * n;
+  bool bad = false;
+  /* W = [(I + Zi Jj)^T | Aj^T]; the solve leaves X^T = (I + Zi Jj)^{-T} Aj^T */
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double s = (p == q) ? 1.0 : 0.0; /* (I + Zi Jj)(q, p) */
+      for (int k = 0; k < n; ++k) s = fma(Xi.Z.at(k * n + q, i), Xj.J.at(p * n + k, j), s);
+      W[q * n + p] = s;                           /* W(p, q) = M(q, p) */
+      W[(n + q) * n + p] = Xj.A.at(p * n + q, j); /* Aj^T(p, q)        */
+    }
+  bad |= solve_square(W, n, n);
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) Xm[q * n + p] = W[(n + p) * n + q]; /* X = (X^T)^T */
+  /* W = [(I + Jj Zi)^T | Ai]; the solve leaves Y^T = (I + Jj Zi)^{-T} Ai */
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double s = (p == q) ? 1.0 : 0.0; /* (I + Jj Zi)(q, p) */
+      for (int k = 0; k < n; ++k) s = fma(Xj.J.at(k * n + q, j), Xi.Z.at(p * n + k, i), s);
+      W[q * n + p] = s;
+      W[(n + q) * n + p] = Xi.A.at(q * n + p, i); /* Ai(p, q) */
+    }
+  bad |= solve_square(W, n, n);
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) Ym[q * n + p] = W[(n + p) * n + q];
+  /* Z = (X Zi) Aj^T + Zj (reads Aj and Zj before they are overwritten) */
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double s = 0.0;
+      for (int k = 0; k < n; ++k) s = fma(Xm[k * n + p], Xi.Z.at(q * n + k, i), s);
+      T[q * n + p] = s;
+    }
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double s = Xj.Z.at(q * n + p, j);
+      for (int k = 0; k < n; ++k) s = fma(T[k * n + p], Xj.A.at(k * n + q, j), s);
+      O.Z.at(q * n + p, o) = s;
+    }
+  /* b = X (bi + Zi ej) + bj */
+  for (int p = 0; p < n; ++p) {
+    double s = Xi.b.at(p, i);
+    for (int k = 0; k < n; ++k) s = fma(Xi.Z.at(k * n + p, i), Xj.e.at(k, j), s);
+    v[p] = s;
+  }
+  for (int p = 0; p < n; ++p) {
+    double s = Xj.b.at(p, j);
+    for (int k = 0; k < n; ++k) s = fma(Xm[k * n + p], v[k], s);
+    O.b.at(p, o) = s;
+  }
+  /* e = Y (ej - Jj bi) + ei */
+  for (int p = 0; p < n; ++p) {
+    double s = Xj.e.at(p, j);
+    for (int k = 0; k < n; ++k) s = fma(-Xj.J.at(k * n + p, j), Xi.b.at(k, i), s);
+    v[p] = s;
+  }
+  for (int p = 0; p < n; ++p) {
+    double s = Xi.e.at(p, i);
+    for (int k = 0; k < n; ++k) s = fma(Ym[k * n + p], v[k], s);
+    O.e.at(p, o) = s;
+  }
+  /* J = Y (Jj Ai) + Ji */
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double s = 0.0;
+      for (int k = 0; k < n; ++k) s = fma(Xj.J.at(k * n + p, j), Xi.A.at(q * n + k, i), s);
+      T[q * n + p] = s;
+    }
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double s = Xi.J.at(q * n + p, i);
+      for (int k = 0; k < n; ++k) s = fma(Ym[k * n + p], T[q * n + k], s);
+      O.J.at(q * n + p, o) = s;
+    }
+  /* A = X Ai (last: overwrites Aj) */
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double s = 0.0;
+      for (int k = 0; k < n; ++k) s = fma(Xm[k * n + p], Xi.A.at(q * n + k, i), s);
+      T[q * n + p] = s;
+    }
+  for (int e = 0; e < n * n; ++e) O.A.at(e, o) = T[e];
+  return bad;
+}
+
+__device__ bool combine_smooth(int n, const SElems& Xi, int64_t i, const SElems& Xj, int64_t j, const SElems& O,
+                               int64_t o, PV ws)
+{
+  /* E = Ej Ei, g = Ej gi + gj, L = Ej Li Ej^T + Lj */
+  PV T = ws, U = ws + n * n;
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double s = 0.0, u = 0.0;
+      for (int k = 0; k < n; ++k) {
+        s = fma(Xj.E.at(k * n + p, j), Xi.L.at(q * n + k, i), s);
+        u = fma(Xj.E.at(k * n + p, j), Xi.E.at(q * n + k, i), u);
+      }
+      T[q * n + p] = s; /* Ej Li */
+      U[q * n + p] = u; /* Ej Ei */
+    }
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double s = Xj.L.at(q * n + p, j);
+      for (int k = 0; k < n; ++k) s = fma(T[k * n + p], Xj.E.at(k * n + q, j), s);
+      O.L.at(q * n + p, o) = s;
+    }
+  for (int p = 0; p < n; ++p) {
+    double s = Xj.g.at(p, j);
+    for (int k = 0; k < n; ++k) s = fma(Xj.E.at(k * n + p, j), Xi.g.at(k, i), s);
+    T[p] = s;
+  }
+  for (int p = 0; p < n; ++p) O.g.at(p, o) = T[p];
+  for (int e = 0; e < n * n; ++e) O.E.at(e, o) = U[e];
+  return false;
+}
+
+template <class El>
+__device__ void copy_elem(int n, const El& X, int64_t i, const El& O, int64_t o);
+
+template <>
+__device__ void copy_elem<FElems>(int n, const FElems& X, int64_t i, const FElems& O, int64_t o)
+{
+  for (int e = 0; e < n * n; ++e) {
+    O.A.at(e, o) = X.A.at(e, i);
+    O.Z.at(e, o) = X.Z.at(e, i);
+    O.J.at(e, o) = X.J.at(e, i);
+  }
+  for (int e = 0; e < n; ++e) {
+    O.b.at(e, o) = X.b.at(e, i);
+    O.e.at(e, o) = X.e.at(e, i);
+  }
+}
+
+template <>
+__device__ void copy_elem<SElems>(int n, const SElems& X, int64_t i, const SElems& O, int64_t o)
+{
+  for (int e = 0; e < n * n; ++e) {
+    O.E.at(e, o) = X.E.at(e, i);
+    O.L.at(e, o) = X.L.at(e, i);
+  }
+  for (int e = 0; e < n; ++e) O.g.at(e, o) = X.g.at(e, i);
+}
+
+__device__ __forceinline__ bool combine(int n, const FElems& Xi, int64_t i, const FElems& Xj, int64_t j,
+                                        const FElems& O, int64_t o, PV ws)
+{
+  return combine_filter(n, Xi, i, Xj, j, O, o, ws);
+}
+__device__ __forceinline__ bool combine(int n, const SElems& Xi, int64_t i, const SElems& Xj, int64_t j,
+                                        const SElems& O, int64_t o, PV ws)
+{
+  return combine_smooth(n, Xi, i, Xj, j, O, o, ws);
+}
+
+/* level tables of a scan: per track, the sequence length L and start at each
+ * level, and prefix sums of items (ceil(L/2) for tracks with L >= 2 in the
+ * up-sweep, ceil(L/2) for tracks with L >= 1 in the down-sweep)             */
+struct ScanLevel {
+  const int64_t* L;
+  const int64_t* start;
+  const int64_t* up_items;   /* [T+1] */
+  const int64_t* down_items; /* [T+1] */
+  int64_t nup, ndown;
+};
+
+/* up-sweep: level d+1 element p = a_{2p} (x) a_{2p+1}, or a_{2p} alone */
+template <class El>
+__global__ void up_kernel(int n, int T, ScanLevel lv, ScanLevel nx, El cur, El nxt, int* flag)
+{
+  extern __shared__ double smem[];
+  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= lv.nup) return;
+  PV ws{smem + threadIdx.x, (int)blockDim.x};
+  const int t = find_track(lv.up_items, T, item);
+  const int64_t p = item - lv.up_items[t];
+  const int64_t s0 = lv.start[t] + 2 * p, o = nx.start[t] + p;
+  if (2 * p + 1 < lv.L[t]) {
+    if (combine(n, cur, s0, cur, s0 + 1, nxt, o, ws)) atomicOr(flag, 2);
+  } else {
+    copy_elem(n, cur, s0, nxt, o);
+  }
+}
+
+/* down-sweep: with level d+1 already inclusive prefixes B,
+ * A_{2p+1} = B_p, A_{2p} = B_{p-1} (x) a_{2p} (A_0 = a_0), in place          */
+template <class El>
+__global__ void down_kernel(int n, int T, ScanLevel lv, ScanLevel nx, El cur, El nxt, int* flag)
+{
+  extern __shared__ double smem[];
+  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= lv.ndown) return;
+  PV ws{smem + threadIdx.x, (int)blockDim.x};
+  const int t = find_track(lv.down_items, T, item);
+  const int64_t p = item - lv.down_items[t];
+  const int64_t L = lv.L[t];
+  if (L < 2) return; /* a one-element sequence is its own prefix */
+  const int64_t s0 = lv.start[t] + 2 * p, b0 = nx.start[t] + p;
+  if (2 * p + 1 < L) copy_elem(n, nxt, b0, cur, s0 + 1);
+  if (p > 0 && combine(n, nxt, b0 - 1, cur, s0, cur, s0, ws)) atomicOr(flag, 2);
+}
+
+/* filtered estimates: step i >= 1 of each track gets (b, Z) of prefix i-1   */
+__global__ void filtered_out_kernel(Args a, FElems el, const int64_t* seq_start, int64_t nsteps)
+{
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nsteps) return;
+  const int n = a.n;
+  const int t = find_track(a.track_start, a.ntracks, g);
+  const int64_t i = g - a.track_start[t];
+  if (i == 0) return;
+  const int64_t r = seq_start[t] + i - 1;
+  for (int p = 0; p < n; ++p) a.state[g * n + p] = el.b.at(p, r);
+  for (int e = 0; e < n * n; ++e) a.cov[g * (int64_t)n * n + e] = el.Z.at(e, r);
+}
+
+/* smoothing elements, reversed: step i of a track of length k is element
+ * r = k-1-i of the track's sequence                                         */
+__global__ void smooth_element_kernel(Args a, Raw raw, SElems out, const int64_t* seq_start, int64_t nsteps)
+{
+  extern __shared__ double smem[];
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nsteps) return;
+  const int n = a.n;
+  const int64_t nn = (int64_t)n * n;
+  const int t = find_track(a.track_start, a.ntracks, g);
+  const int64_t g0 = a.track_start[t], k = a.track_start[t + 1] - g0, i = g - g0;
+  const int64_t r = seq_start[t] + (k - 1 - i);
+  const double* x = a.state + g * n;
+  const double* P = a.cov + g * nn;
+  if (i == k - 1) {
+    for (int e = 0; e < n * n; ++e) {
+      out.E.at(e, r) = 0.0;
+      out.L.at(e, r) = P[e];
+    }
+    for (int p = 0; p < n; ++p) out.g.at(p, r) = x[p];
+    return;
+  }
+  PV ws{smem + threadIdx.x, (int)blockDim.x};
+  /* ws: Q (nn) | PFt (nn) | W (2nn) | v (n) | cov ws (2nn) */
+  PV Q = ws, PFt = ws + n * n, W = PFt + n * n, v = W + 2 * n * n, cw = v + n;
+  const int64_t g1 = g + 1;
+  const double* F = raw.F + g1 * nn;
+  const double* c = raw.c + g1 * n;
+  bool bad = explicit_cov(raw.K_type[g1], raw.K + g1 * nn, n, n, Q, cw);
+  /* PFt = P F^T */
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double s = 0.0;
+      for (int k2 = 0; k2 < n; ++k2) s = fma(P[k2 * n + p], F[k2 * n + q], s);
+      PFt[q * n + p] = s;
+    }
+  /* W = [ (F P F^T + Q)^T | (P F^T)^T ]; solve gives E^T */
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double s = Q[q * n + p];
+      for (int k2 = 0; k2 < n; ++k2) s = fma(F[k2 * n + p], PFt[q * n + k2], s);
+      W[p * n + q] = s; /* transpose */
+      W[(n + q) * n + p] = PFt[p * n + q];
+    }
+  bad |= solve_square(W, n, n);
+  PV E = Q; /* E = (E^T)^T, reuse Q */
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) E[q * n + p] = W[(n + p) * n + q];
+  /* g = x - E (F x + c) */
+  for (int p = 0; p < n; ++p) {
+    double s = c[p];
+    for (int k2 = 0; k2 < n; ++k2) s = fma(F[k2 * n + p], x[k2], s);
+    v[p] = s;
+  }
+  for (int p = 0; p < n; ++p) {
+    double s = x[p];
+    for (int k2 = 0; k2 < n; ++k2) s = fma(-E[k2 * n + p], v[k2], s);
+    out.g.at(p, r) = s;
+  }
+  /* L = P - (E F) P */
+  PV EF = PFt;
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double s = 0.0;
+      for (int k2 = 0; k2 < n; ++k2) s = fma(E[k2 * n + p], F[q * n + k2], s);
+      EF[q * n + p] = s;
+    }
+  for (int q = 0; q < n; ++q)
+    for (int p = 0; p < n; ++p) {
+      double s = P[q * n + p];
+      for (int k2 = 0; k2 < n; ++k2) s = fma(-EF[k2 * n + p], P[q * n + k2], s);
+      out.L.at(q * n + p, r) = s;
+    }
+  for (int e = 0; e < n * n; ++e) out.E.at(e, r) = E[e];
+  if (bad) atomicOr(a.flag, 2);
+}
+
+__global__ void smoothed_out_kernel(Args a, SElems el, const int64_t* seq_start, int64_t nsteps)
+{
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nsteps) return;
+  const int n = a.n;
+  const int t = find_track(a.track_start, a.ntracks, g);
+  const int64_t g0 = a.track_start[t], k = a.track_start[t + 1] - g0, i = g - g0;
+  const int64_t r = seq_start[t] + (k - 1 - i);
+  for (int p = 0; p < n; ++p) a.state[g * n + p] = el.g.at(p, r);
+  for (int e = 0; e < n * n; ++e) a.cov[g * (int64_t)n * n + e] = el.L.at(e, r);
+}
+
+/* ---------------------------------------------------------------------------
+ * host side
+ * ------------------------------------------------------------------------ */
+struct Workspace {
+  int device = -1;
+  void* dev = nullptr;
+  size_t bytes = 0;
+};
+thread_local Workspace tl_ws;
+
+int ensure(size_t bytes, void** out)
+{
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (tl_ws.dev && (tl_ws.bytes < bytes || tl_ws.device != dev)) {
+    cudaFree(tl_ws.dev);
+    tl_ws = Workspace();
+  }
+  if (!tl_ws.dev) {
+    size_t want = bytes + (bytes >> 3);
+    if (cudaMalloc(&tl_ws.dev, want) != cudaSuccess) {
+      cudaGetLastError();
+      tl_ws = Workspace();
+      return ukg_set_error(KALMAN_GPU_ENOMEM, "cudaMalloc of %zu bytes of workspace failed", want);
+    }
+    tl_ws.bytes = want;
+    tl_ws.device = dev;
+  }
+  *out = tl_ws.dev;
+  return 0;
+}
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+int pick_block(size_t per_thread, int preferred, int* block)
+{
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  int bs = preferred;
+  while (bs > 32 && (size_t)bs * per_thread > (size_t)optin / 2) bs /= 2;
+  while (bs > 1 && (size_t)bs * per_thread > (size_t)optin) bs /= 2;
+  if ((size_t)bs * per_thread > (size_t)optin) return -1;
+  *block = bs;
+  return 0;
+}
+
+/* host-side plan of one scan: per level, the per-track tables (flattened) */
+struct ScanPlan {
+  int nlev = 0;
+  std::vector<int64_t> cap;          /* elements per level */
+  std::vector<size_t> off_L, off_start, off_up, off_down;
+  std::vector<int64_t> nup, ndown;
+};
+
+void plan_scan(const std::vector<int64_t>& L0, ScanPlan& sp, std::vector<int64_t>& tab)
+{
+  const int T = (int)L0.size();
+  std::vector<int64_t> L = L0;
+  for (;;) {
+    sp.off_L.push_back(tab.size());
+    tab.insert(tab.end(), L.begin(), L.end());
+    sp.off_start.push_back(tab.size());
+    int64_t s = 0;
+    for (int t = 0; t < T; ++t) { tab.push_back(s); s += L[t]; }
+    sp.cap.push_back(s);
+    sp.off_up.push_back(tab.size());
+    int64_t acc = 0;
+    for (int t = 0; t < T; ++t) { tab.push_back(acc); acc += L[t] >= 2 ? (L[t] + 1) / 2 : 0; }
+    tab.push_back(acc);
+    sp.nup.push_back(acc);
+    sp.off_down.push_back(tab.size());
+    acc = 0;
+    for (int t = 0; t < T; ++t) { tab.push_back(acc); acc += L[t] >= 2 ? (L[t] + 1) / 2 : 0; }
+    tab.push_back(acc);
+    sp.ndown.push_back(acc);
+    sp.nlev++;
+    bool more = false;
+    for (int t = 0; t < T; ++t) {
+      L[t] = L[t] >= 2 ? (L[t] + 1) / 2 : L[t];
+      more |= L[t] >= 2;
+    }
+    if (!more) {
+      /* one more level: every track's full reduction sits here */
+      sp.off_L.push_back(tab.size());
+      tab.insert(tab.end(), L.begin(), L.end());
+      sp.off_start.push_back(tab.size());
+      s = 0;
+      for (int t = 0; t < T; ++t) { tab.push_back(s); s += L[t]; }
+      sp.cap.push_back(s);
+      sp.off_up.push_back(tab.size());
+      for (int t = 0; t <= T; ++t) tab.push_back(0);
+      sp.nup.push_back(0);
+      sp.off_down.push_back(tab.size());
+      for (int t = 0; t <= T; ++t) tab.push_back(0);
+      sp.ndown.push_back(0);
+      sp.nlev++;
+      break;
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" void ukg_release_associative_workspace(void)
+{
+  if (tl_ws.dev) cudaFree(tl_ws.dev);
+  tl_ws = Workspace();
+}
 
 extern "C" int ukg_associative_device(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream)
 {
-  (void)options; (void)p; (void)cuda_stream;
-  return ukg_set_error(KALMAN_GPU_EINVAL, "the associative smoother is not built yet");
+  (void)options;
+  cudaStream_t st = (cudaStream_t)cuda_stream;
+  const int n = p->n, T = p->ntracks;
+  const int64_t nn = (int64_t)n * n, N = p->nsteps;
+  if (!p->covariance)
+    return ukg_set_error(KALMAN_GPU_EINVAL, "the associative smoother needs the covariance output array (the "
+                         "filtered covariances feed the smoothing elements)");
+  const int mx = p->mmax > n ? p->mmax : n;
+
+  std::vector<int64_t> tab, Lf(T), Ls(T);
+  for (int t = 0; t < T; ++t) {
+    const int64_t k = p->track_start[t + 1] - p->track_start[t];
+    Lf[t] = k > 0 ? k - 1 : 0;
+    Ls[t] = k;
+  }
+  ScanPlan fp, sp;
+  plan_scan(Lf, fp, tab);
+  plan_scan(Ls, sp, tab);
+  const size_t off_ts = tab.size();
+  tab.insert(tab.end(), p->track_start, p->track_start + T + 1);
+
+  /* workspace: tables, flag, filtering levels (3nn + 2n per element),
+     smoothing levels reuse the same region (2nn + n per element)            */
+  size_t bytes = 0;
+  auto take = [&](size_t b) { size_t o = bytes; bytes = align_up(bytes + b, 256); return o; };
+  const size_t o_tab = take(tab.size() * sizeof(int64_t));
+  const size_t o_flag = take(sizeof(int));
+  std::vector<size_t> o_fl(fp.nlev), o_sl(sp.nlev);
+  const size_t lev_base = bytes;
+  for (int l = 0; l < fp.nlev; ++l) o_fl[l] = take((size_t)std::max<int64_t>(fp.cap[l], 1) * (3 * nn + 2 * n) * 8);
+  const size_t f_end = bytes;
+  bytes = lev_base;
+  for (int l = 0; l < sp.nlev; ++l) o_sl[l] = take((size_t)std::max<int64_t>(sp.cap[l], 1) * (2 * nn + n) * 8);
+  bytes = std::max(bytes, f_end);
+  void* base = nullptr;
+  if (int e = ensure(bytes, &base)) return e;
+  char* B = (char*)base;
+  int64_t* dtab = (int64_t*)(B + o_tab);
+  int* dflag = (int*)(B + o_flag);
+  cudaMemcpyAsync(dtab, tab.data(), tab.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(dflag, 0, sizeof(int), st);
+
+  auto felems = [&](int l) {
+    const int64_t c = std::max<int64_t>(fp.cap[l], 1);
+    double* d = (double*)(B + o_fl[l]);
+    FElems e;
+    e.A = Soa{d, c};
+    e.Z = Soa{d + nn * c, c};
+    e.J = Soa{d + 2 * nn * c, c};
+    e.b = Soa{d + 3 * nn * c, c};
+    e.e = Soa{d + (3 * nn + n) * c, c};
+    return e;
+  };
+  auto selems = [&](int l) {
+    const int64_t c = std::max<int64_t>(sp.cap[l], 1);
+    double* d = (double*)(B + o_sl[l]);
+    SElems e;
+    e.E = Soa{d, c};
+    e.L = Soa{d + nn * c, c};
+    e.g = Soa{d + 2 * nn * c, c};
+    return e;
+  };
+  auto level = [&](const ScanPlan& s, int l) {
+    ScanLevel v;
+    v.L = dtab + s.off_L[l];
+    v.start = dtab + s.off_start[l];
+    v.up_items = dtab + s.off_up[l];
+    v.down_items = dtab + s.off_down[l];
+    v.nup = s.nup[l];
+    v.ndown = s.ndown[l];
+    return v;
+  };
+
+  Args a;
+  a.n = n;
+  a.ntracks = T;
+  a.track_start = dtab + off_ts;
+  a.state = p->state;
+  a.cov = p->covariance;
+  a.flag = dflag;
+  Raw raw{p->F, p->c, p->K, p->G, p->o, p->C, p->K_type, p->C_type, p->obs_rows, p->mmax};
+
+  /* element_kernel: m0 | P0 | Kx | scratch = max(step-0 estimate, explicit K,
+     F P0, observation update)                                                */
+  const size_t sc_obs = 3 * (size_t)mx * mx + (size_t)mx * (mx + n) + 2 * (size_t)n * mx + mx + n + nn;
+  const size_t sc_elem = std::max<size_t>(std::max<size_t>((size_t)n * (n + 1) + nn + n, 2 * nn), sc_obs);
+  const size_t pt_elem = ((size_t)n + 2 * nn + sc_elem + 8) * 8;
+  const size_t pt_comb = (size_t)(5 * nn + n + 8) * 8;
+  const size_t pt_selem = (size_t)(6 * nn + n + 8) * 8;
+  int be, bc, bsm;
+  if (pick_block(pt_elem, 64, &be) || pick_block(pt_comb, 64, &bc) || pick_block(pt_selem, 64, &bsm))
+    return ukg_set_error(KALMAN_GPU_EINVAL, "state dimension %d needs more shared memory per thread than this build "
+                         "of the associative kernels uses", n);
+  cudaFuncSetAttribute(element_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(be * pt_elem));
+  cudaFuncSetAttribute(up_kernel<FElems>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bc * pt_comb));
+  cudaFuncSetAttribute(down_kernel<FElems>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bc * pt_comb));
+  cudaFuncSetAttribute(up_kernel<SElems>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bc * pt_comb));
+  cudaFuncSetAttribute(down_kernel<SElems>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bc * pt_comb));
+  cudaFuncSetAttribute(smooth_element_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bsm * pt_selem));
+  auto grid = [](int64_t items, int block) { return (unsigned)((items + block - 1) / block); };
+  const int ew = 128;
+
+  /* filtering elements and the forward scan */
+  const int64_t* fstart0 = dtab + fp.off_start[0];
+  UKG_LAUNCH(UKG_K_AS_ELEMENT, st,
+             (element_kernel<<<grid(N, be), be, be * pt_elem, st>>>(a, raw, felems(0), fstart0, N, mx)));
+  for (int l = 0; l + 1 < fp.nlev; ++l)
+    if (fp.nup[l] > 0)
+      UKG_LAUNCH(UKG_K_AS_SCAN, st,
+                 (up_kernel<FElems><<<grid(fp.nup[l], bc), bc, bc * pt_comb, st>>>(
+                     n, T, level(fp, l), level(fp, l + 1), felems(l), felems(l + 1), dflag)));
+  for (int l = fp.nlev - 2; l >= 0; --l)
+    if (fp.ndown[l] > 0)
+      UKG_LAUNCH(UKG_K_AS_SCAN, st,
+                 (down_kernel<FElems><<<grid(fp.ndown[l], bc), bc, bc * pt_comb, st>>>(
+                     n, T, level(fp, l), level(fp, l + 1), felems(l), felems(l + 1), dflag)));
+  UKG_LAUNCH(UKG_K_AS_ELEMENT, st, (filtered_out_kernel<<<grid(N, ew), ew, 0, st>>>(a, felems(0), fstart0, N)));
+  /* smoothing elements and the reverse scan */
+  const int64_t* sstart0 = dtab + sp.off_start[0];
+  UKG_LAUNCH(UKG_K_AS_SMOOTH, st,
+             (smooth_element_kernel<<<grid(N, bsm), bsm, bsm * pt_selem, st>>>(a, raw, selems(0), sstart0, N)));
+  for (int l = 0; l + 1 < sp.nlev; ++l)
+    if (sp.nup[l] > 0)
+      UKG_LAUNCH(UKG_K_AS_SCAN, st,
+                 (up_kernel<SElems><<<grid(sp.nup[l], bc), bc, bc * pt_comb, st>>>(
+                     n, T, level(sp, l), level(sp, l + 1), selems(l), selems(l + 1), dflag)));
+  for (int l = sp.nlev - 2; l >= 0; --l)
+    if (sp.ndown[l] > 0)
+      UKG_LAUNCH(UKG_K_AS_SCAN, st,
+                 (down_kernel<SElems><<<grid(sp.ndown[l], bc), bc, bc * pt_comb, st>>>(
+                     n, T, level(sp, l), level(sp, l + 1), selems(l), selems(l + 1), dflag)));
+  UKG_LAUNCH(UKG_K_AS_SMOOTH, st, (smoothed_out_kernel<<<grid(N, ew), ew, 0, st>>>(a, selems(0), sstart0, N)));
+
+  int hflag = 0;
+  cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return ukg_set_error(KALMAN_GPU_ECUDA, "associative smoother: %s", cudaGetErrorString(e));
+  ukg_prof_collect();
+  if (hflag & 4) return ukg_set_error(KALMAN_GPU_EINVAL, "malformed input: the associative smoother needs a square "
+                                     "observation at the first step of every track, observation rows within "
+                                     "[0, mmax] and known covariance types");
+  if (hflag & 2) return ukg_set_error(KALMAN_GPU_ESINGULAR, "a singular matrix in the associative smoother");
+  return 0;
 }

@@ -611,44 +611,92 @@ __global__ void solve_kernel(Args a, int want_cov)
 /* ---------------------------------------------------------------------------
  * host side: plan, workspace, launches
  * ------------------------------------------------------------------------ */
+constexpr int kMaxLevels = 64;
+
 struct LevelPlan {
   int64_t S = 0, E = 0, npairs = 0, nsolve = 0, ntail = 0;
   size_t off_L = 0, off_slot = 0, off_pair = 0, off_solve = 0, off_tail = 0; /* in int64 entries */
 };
 
-struct Workspace {
-  int device = -1;
-  void* dev = nullptr;
-  size_t dev_bytes = 0;
+/* Everything the launches need besides the arrays: per-level track tables
+ * (host copy, uploaded into the workspace) and the workspace layout.        */
+struct Plan {
+  int nlev = 0;
+  LevelPlan lp[kMaxLevels];
+  size_t tab_entries = 0, off_ts = 0;
+  size_t o_tab = 0, o_flag = 0, o_eq[2] = {0, 0}, o_m[2] = {0, 0}, o_rec[kMaxLevels] = {0}, o_U[kMaxLevels] = {0};
+  size_t bytes = 0;
+  int64_t S0 = 0, S1 = 0;
 };
-thread_local Workspace tl_ws; /* one cached device arena per host thread */
-
-int ensure_workspace(size_t bytes, void** out)
-{
-  int dev = 0;
-  cudaGetDevice(&dev);
-  Workspace& w = tl_ws;
-  if (w.dev && (w.dev_bytes < bytes || w.device != dev)) {
-    cudaFree(w.dev);
-    w.dev = nullptr;
-    w.dev_bytes = 0;
-  }
-  if (!w.dev) {
-    size_t want = bytes + (bytes >> 3);
-    cudaError_t e = cudaMalloc(&w.dev, want);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      return ukg_set_error(KALMAN_GPU_ENOMEM, "cudaMalloc of %zu bytes of workspace failed: %s", want,
-                           cudaGetErrorString(e));
-    }
-    w.dev_bytes = want;
-    w.device = dev;
-  }
-  *out = w.dev;
-  return 0;
-}
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+/* Builds the plan.  Track t has k_t >> l steps at level l.  When tab is not
+ * NULL the tables are written into it (tab_cap entries).  Returns the number
+ * of table entries needed, or 0 if the recursion is deeper than kMaxLevels. */
+size_t build_plan(const kalman_gpu_problem_t* p, bool want_cov, Plan& P, int64_t* tab, size_t tab_cap)
+{
+  const int n = p->n, T = p->ntracks;
+  const int mx = p->mmax > n ? p->mmax : n;
+  const int64_t nn = (int64_t)n * n;
+  int64_t kmax = 0;
+  for (int t = 0; t < T; ++t) kmax = std::max<int64_t>(kmax, p->track_start[t + 1] - p->track_start[t]);
+  P.nlev = 1;
+  for (int64_t L = kmax; L > 1; L /= 2) ++P.nlev;
+  if (P.nlev > kMaxLevels) return 0;
+  size_t pos = 0;
+  auto put = [&](int64_t v) {
+    if (tab && pos < tab_cap) tab[pos] = v;
+    ++pos;
+  };
+  auto len = [&](int t, int l) { return (p->track_start[t + 1] - p->track_start[t]) >> l; };
+  for (int l = 0; l < P.nlev; ++l) {
+    LevelPlan& L = P.lp[l];
+    L = LevelPlan();
+    L.off_L = pos;
+    for (int t = 0; t < T; ++t) put(len(t, l));
+    L.off_slot = pos;
+    int64_t s = 0;
+    for (int t = 0; t < T; ++t) { put(s); s += (len(t, l) + 1) & ~int64_t(1); }
+    L.S = s;
+    L.off_pair = pos;
+    int64_t acc = 0;
+    for (int t = 0; t < T; ++t) { put(acc); const int64_t k = len(t, l); acc += k >= 2 ? k / 2 : 0; }
+    put(acc);
+    L.npairs = acc;
+    L.off_solve = pos;
+    acc = 0;
+    for (int t = 0; t < T; ++t) { put(acc); const int64_t k = len(t, l); acc += k >= 2 ? (k + 1) / 2 : 0; }
+    put(acc);
+    L.nsolve = L.E = acc;
+    L.off_tail = pos;
+    for (int t = 0; t < T; ++t)
+      if (len(t, l) & 1) { put(t); ++L.ntail; }
+  }
+  P.off_ts = pos;
+  for (int t = 0; t <= T; ++t) put(p->track_start[t]);
+  P.tab_entries = pos;
+
+  /* workspace layout; level equations ping-pong between two regions sized
+     for levels 0 and 1, records and off-diagonal blocks per level           */
+  size_t bytes = 0;
+  auto take = [&](size_t b) { size_t o = bytes; bytes = align_up(bytes + b, 256); return o; };
+  P.o_tab = take(pos * sizeof(int64_t));
+  P.o_flag = take(sizeof(int));
+  const int64_t eq_doubles_per_slot = 2 * nn + n + (int64_t)mx * n + mx;
+  P.S0 = P.lp[0].S;
+  P.S1 = P.nlev > 1 ? P.lp[1].S : 0;
+  P.o_eq[0] = take((size_t)std::max<int64_t>(P.S0, 1) * eq_doubles_per_slot * sizeof(double));
+  P.o_m[0] = take((size_t)std::max<int64_t>(P.S0, 1) * sizeof(int32_t));
+  P.o_eq[1] = take((size_t)std::max<int64_t>(P.S1, 1) * eq_doubles_per_slot * sizeof(double));
+  P.o_m[1] = take((size_t)std::max<int64_t>(P.S1, 1) * sizeof(int32_t));
+  for (int l = 0; l < P.nlev; ++l) {
+    P.o_rec[l] = take((size_t)std::max<int64_t>(P.lp[l].E, 1) * (3 * nn + n) * sizeof(double));
+    P.o_U[l] = (want_cov && l > 0) ? take((size_t)std::max<int64_t>(P.lp[l].S, 1) * nn * sizeof(double)) : 0;
+  }
+  P.bytes = bytes;
+  return pos;
+}
 
 int pick_block(size_t per_thread_bytes, int preferred, int* block)
 {
@@ -666,118 +714,49 @@ int pick_block(size_t per_thread_bytes, int preferred, int* block)
   return 0;
 }
 
-}  // namespace
-
-extern "C" void ukg_release_oddeven_workspace(void)
+/* Uploads the tables, runs every kernel of the smoother on stream st using
+ * the device workspace at B (at least P.bytes), waits, reports the flags.   */
+int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, const Plan& P, const int64_t* tab,
+             char* B)
 {
-  if (tl_ws.dev) cudaFree(tl_ws.dev);
-  tl_ws = Workspace();
-}
-
-extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream)
-{
-  cudaStream_t st = (cudaStream_t)cuda_stream;
-  const int n = p->n, T = p->ntracks;
+  const int n = p->n, T = p->ntracks, nlev = P.nlev;
   const int mx = p->mmax > n ? p->mmax : n;
   const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
   const int64_t nn = (int64_t)n * n;
-
-  /* ---- plan: per-level track tables ---- */
-  std::vector<int64_t> Lcur(T);
-  int64_t kmax = 0;
-  for (int t = 0; t < T; ++t) {
-    Lcur[t] = p->track_start[t + 1] - p->track_start[t];
-    kmax = std::max(kmax, Lcur[t]);
-  }
-  if (p->nsteps == 0) return 0;
-  int nlev = 1;
-  for (int64_t L = kmax; L > 1; L /= 2) ++nlev;
-  std::vector<LevelPlan> lp(nlev);
-  std::vector<int64_t> tab;
-  std::vector<int64_t> Ls = Lcur;
-  for (int l = 0; l < nlev; ++l) {
-    LevelPlan& P = lp[l];
-    P.off_L = tab.size();
-    tab.insert(tab.end(), Ls.begin(), Ls.end());
-    P.off_slot = tab.size();
-    int64_t s = 0;
-    for (int t = 0; t < T; ++t) { tab.push_back(s); s += (Ls[t] + 1) & ~int64_t(1); }
-    P.S = s;
-    P.off_pair = tab.size();
-    int64_t acc = 0;
-    for (int t = 0; t < T; ++t) { tab.push_back(acc); acc += Ls[t] >= 2 ? Ls[t] / 2 : 0; }
-    tab.push_back(acc);
-    P.npairs = acc;
-    P.off_solve = tab.size();
-    acc = 0;
-    for (int t = 0; t < T; ++t) { tab.push_back(acc); acc += Ls[t] >= 2 ? (Ls[t] + 1) / 2 : 0; }
-    tab.push_back(acc);
-    P.nsolve = P.E = acc;
-    P.off_tail = tab.size();
-    for (int t = 0; t < T; ++t)
-      if (Ls[t] & 1) tab.push_back(t);
-    P.ntail = (int64_t)tab.size() - (int64_t)P.off_tail;
-    for (int t = 0; t < T; ++t) Ls[t] /= 2;
-  }
-  tab.insert(tab.end(), p->track_start, p->track_start + T + 1);
-  const size_t off_ts = tab.size() - (T + 1);
-
-  /* ---- workspace layout ---- */
-  size_t bytes = 0;
-  auto take = [&](size_t b) { size_t o = bytes; bytes = align_up(bytes + b, 256); return o; };
-  const size_t o_tab = take(tab.size() * sizeof(int64_t));
-  const size_t o_flag = take(sizeof(int));
-  /* level equations: ping-pong between two regions sized for levels 0 and 1 */
-  const int64_t eq_doubles_per_slot = 2 * nn + n + (int64_t)mx * n + mx;
-  const int64_t S0 = lp[0].S, S1 = nlev > 1 ? lp[1].S : 0;
-  size_t o_eq[2], o_m[2];
-  o_eq[0] = take((size_t)S0 * eq_doubles_per_slot * sizeof(double));
-  o_m[0] = take((size_t)S0 * sizeof(int32_t));
-  o_eq[1] = take((size_t)std::max<int64_t>(S1, 1) * eq_doubles_per_slot * sizeof(double));
-  o_m[1] = take((size_t)std::max<int64_t>(S1, 1) * sizeof(int32_t));
-  std::vector<size_t> o_rec(nlev), o_U(nlev);
-  for (int l = 0; l < nlev; ++l) {
-    o_rec[l] = take((size_t)std::max<int64_t>(lp[l].E, 1) * (3 * nn + n) * sizeof(double));
-    o_U[l] = (want_cov && l > 0) ? take((size_t)std::max<int64_t>(lp[l].S, 1) * nn * sizeof(double)) : 0;
-  }
-  void* base = nullptr;
-  if (int e = ensure_workspace(bytes, &base)) return e;
-  char* B = (char*)base;
-  int64_t* dtab = (int64_t*)(B + o_tab);
-  int* dflag = (int*)(B + o_flag);
-  cudaMemcpyAsync(dtab, tab.data(), tab.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+  const LevelPlan* lp = P.lp;
+  int64_t* dtab = (int64_t*)(B + P.o_tab);
+  int* dflag = (int*)(B + P.o_flag);
+  cudaMemcpyAsync(dtab, tab, P.tab_entries * sizeof(int64_t), cudaMemcpyHostToDevice, st);
   cudaMemsetAsync(dflag, 0, sizeof(int), st);
 
   auto level_dev = [&](int l) {
     LevelDev d;
     memset(&d, 0, sizeof(d));
     if (l >= nlev) return d;
-    const LevelPlan& P = lp[l];
-    const int64_t S = l < 2 ? (l == 0 ? S0 : S1) : P.S; /* stride: region capacity */
-    const int64_t Sr = (l & 1) ? std::max<int64_t>(S1, 1) : S0;
-    (void)S;
-    double* eq = (double*)(B + o_eq[l & 1]);
+    const LevelPlan& L = lp[l];
+    const int64_t Sr = (l & 1) ? std::max<int64_t>(P.S1, 1) : std::max<int64_t>(P.S0, 1); /* region stride */
+    double* eq = (double*)(B + P.o_eq[l & 1]);
     d.F = Soa{eq, Sr};
     d.H = Soa{eq + nn * Sr, Sr};
     d.c = Soa{eq + 2 * nn * Sr, Sr};
     d.G = Soa{eq + (2 * nn + n) * Sr, Sr};
     d.o = Soa{eq + (2 * nn + n + (int64_t)mx * n) * Sr, Sr};
-    d.m = (int32_t*)(B + o_m[l & 1]);
-    const int64_t E = std::max<int64_t>(P.E, 1);
-    double* rec = (double*)(B + o_rec[l]);
+    d.m = (int32_t*)(B + P.o_m[l & 1]);
+    const int64_t E = std::max<int64_t>(L.E, 1);
+    double* rec = (double*)(B + P.o_rec[l]);
     d.R = Soa{rec, E};
     d.Ft = Soa{rec + nn * E, E};
     d.Y = Soa{rec + 2 * nn * E, E};
     d.cr = Soa{rec + 3 * nn * E, E};
-    d.U = (want_cov && l > 0) ? Soa{(double*)(B + o_U[l]), std::max<int64_t>(P.S, 1)} : Soa{nullptr, 0};
-    d.L = dtab + P.off_L;
-    d.slot = dtab + P.off_slot;
-    d.pair = dtab + P.off_pair;
-    d.solve = dtab + P.off_solve;
-    d.tail = dtab + P.off_tail;
-    d.npairs = P.npairs;
-    d.nsolve = P.nsolve;
-    d.ntail = P.ntail;
+    d.U = (want_cov && l > 0) ? Soa{(double*)(B + P.o_U[l]), std::max<int64_t>(L.S, 1)} : Soa{nullptr, 0};
+    d.L = dtab + L.off_L;
+    d.slot = dtab + L.off_slot;
+    d.pair = dtab + L.off_pair;
+    d.solve = dtab + L.off_solve;
+    d.tail = dtab + L.off_tail;
+    d.npairs = L.npairs;
+    d.nsolve = L.nsolve;
+    d.ntail = L.ntail;
     return d;
   };
 
@@ -786,7 +765,7 @@ extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* 
   a.n = n;
   a.mx = mx;
   a.ntracks = T;
-  a.track_start = dtab + off_ts;
+  a.track_start = dtab + P.off_ts;
   a.state = p->state;
   a.cov = want_cov ? p->covariance : nullptr;
   a.flag = dflag;
@@ -845,4 +824,60 @@ extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* 
   if (hflag & 1) return ukg_set_error(KALMAN_GPU_ESINGULAR, "a covariance factor is not positive definite");
   if (hflag & 2) return ukg_set_error(KALMAN_GPU_ESINGULAR, "zero pivot: the smoothing problem is not observable");
   return 0;
+}
+
+/* cached device workspace and plan tables of the ordinary entry point */
+struct Workspace {
+  int device = -1;
+  void* dev = nullptr;
+  size_t dev_bytes = 0;
+};
+thread_local Workspace tl_ws; /* one cached device arena per host thread */
+thread_local std::vector<int64_t> tl_tab;
+
+int ensure_workspace(size_t bytes, void** out)
+{
+  int dev = 0;
+  cudaGetDevice(&dev);
+  Workspace& w = tl_ws;
+  if (w.dev && (w.dev_bytes < bytes || w.device != dev)) {
+    cudaFree(w.dev);
+    w.dev = nullptr;
+    w.dev_bytes = 0;
+  }
+  if (!w.dev) {
+    size_t want = bytes + (bytes >> 3);
+    cudaError_t e = cudaMalloc(&w.dev, want);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return ukg_set_error(KALMAN_GPU_ENOMEM, "cudaMalloc of %zu bytes of workspace failed: %s", want,
+                           cudaGetErrorString(e));
+    }
+    w.dev_bytes = want;
+    w.device = dev;
+  }
+  *out = w.dev;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" void ukg_release_oddeven_workspace(void)
+{
+  if (tl_ws.dev) cudaFree(tl_ws.dev);
+  tl_ws = Workspace();
+}
+
+extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream)
+{
+  if (p->nsteps == 0) return 0;
+  const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
+  Plan P;
+  const size_t need = build_plan(p, want_cov, P, nullptr, 0);
+  if (need == 0) return ukg_set_error(KALMAN_GPU_EINVAL, "tracks longer than 2^%d steps", kMaxLevels - 1);
+  tl_tab.resize(need);
+  build_plan(p, want_cov, P, tl_tab.data(), need);
+  void* base = nullptr;
+  if (int e = ensure_workspace(P.bytes, &base)) return e;
+  return run_plan(options, p, (cudaStream_t)cuda_stream, P, tl_tab.data(), (char*)base);
 }
