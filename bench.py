@@ -15,8 +15,8 @@ covariances, FP64) of every track, through the library's C ABI:
   e2e   -- the same call handed page-locked HOST arrays: host->device copy of
            the equations, smoothing, device->host copy of states and
            covariances all inside the timed region.
-Other keys: per-kernel roofline (FP64 pipe: the kernels are arithmetic-bound,
-see the design doc), CPU baseline (the oracle's C restatement of the reference
+Other keys: per-kernel roofline (FP64 pipe: the kernels are arithmetic-bound),
+CPU baseline (the oracle's C restatement of the reference
 smoother on all host cores, a bounded sample of the same tracks), clocks.
 
 --impl reference: times the CPU restatement of the reference's odd-even

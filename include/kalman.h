@@ -12,7 +12,7 @@
  *   kalman_create ... kalman_perftest          c/kalman.h:117-142
  *   kalman_smooth_oddeven / _associative       c/kalman.h:148-149
  *
- * Differences a client can observe (all documented in the design doc):
+ * Differences a client can observe:
  *  - kalman_t is opaque here; the reference exposes its vtable struct, but no
  *    client touches its fields.
  *  - The library implements KALMAN_ALGORITHM_ODDEVEN and _ASSOCIATIVE on the

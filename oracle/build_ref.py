@@ -37,6 +37,11 @@ SOURCES = [
 HEADERS = ["kalman.h", "matrix_ops.h", "flexible_arrays.h", "parallel.h", "concurrent_set.h", "memory.h"]
 
 
+def sources_present():
+    """True where the reference sources exist (the build machine only)."""
+    return os.path.isdir(REF_C)
+
+
 def find_openblas():
     import scipy
     libs = glob.glob(os.path.join(os.path.dirname(scipy.__file__), "..", "scipy.libs", "libscipy_openblas*.so"))

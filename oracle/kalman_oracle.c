@@ -26,9 +26,9 @@
  * dgeqrf + dormqr('L','T') compute.  Reflectors follow LAPACK dlarfg's sign
  * convention, so R matches LAPACK's up to rounding.
  *
- * Extensions beyond the reference, where the reference aborts (documented in
- * the design doc): a pair of consecutive unobserved steps, and an unobserved last
- * step of an odd-length level, are handled by carrying empty observation
+ * Extensions beyond the reference, where the reference aborts: a pair of
+ * consecutive unobserved steps, and an unobserved last step of an odd-length
+ * level, are handled by carrying empty observation
  * blocks instead of calling QR on NULL.
  *
  * Associative smoother (c/kalman_associative_smoother.c):
