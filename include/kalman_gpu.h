@@ -117,6 +117,22 @@ int64_t kalman_gpu_launch_count(void);
  * for roofline reporting; takes a few milliseconds.                          */
 double  kalman_gpu_measure_fp64_tflops(int active_lanes);
 
+/* Allocation-free odd-even smoothing of a packed problem held in DEVICE
+ * memory.  No counterpart in the reference: it exists for callers that must
+ * not allocate device memory while they run -- real-time tracking loops with
+ * a no-allocation rule (cudaMalloc/cudaFree may synchronize the device and
+ * take unbounded time) and plugins whose host program owns all device memory.
+ * The smoother's scratch comes from a fixed array of
+ * KALMAN_GPU_NOALLOC_SCRATCH_BYTES that every device loading the library
+ * holds until the process exits (about 24,000 steps of a 6-state model with
+ * covariances fit); larger problems are rejected with KALMAN_GPU_EINVAL.  The
+ * caller passes the input and output arrays.  The first call on a device looks
+ * up the array's device address (make it before any stream capture).  Calls
+ * share the array: they are serialized and each waits for its kernels; work
+ * that overlapped a call on the GPU would race on it.                        */
+#define KALMAN_GPU_NOALLOC_SCRATCH_BYTES (64u << 20)
+int kalman_gpu_smooth_oddeven_noalloc(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream);
+
 /* Releases the device workspace and pinned staging buffers cached by the
  * library for the current device.                                            */
 void kalman_gpu_release(void);

@@ -43,6 +43,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "profiling.h"
@@ -880,4 +881,81 @@ extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* 
   void* base = nullptr;
   if (int e = ensure_workspace(P.bytes, &base)) return e;
   return run_plan(options, p, (cudaStream_t)cuda_stream, P, tl_tab.data(), (char*)base);
+}
+
+/* ---------------------------------------------------------------------------
+ * Allocation-free entry point (kalman_gpu_smooth_oddeven_noalloc).
+ *
+ * For callers that must not allocate device memory once they are running --
+ * real-time tracking loops with a no-allocation rule (cudaMalloc and cudaFree
+ * can synchronize the device and take unbounded time) and plugins whose host
+ * program owns all device memory through its own allocator -- this variant of
+ * the odd-even smoother takes its scratch (track tables, flags, level
+ * equations, back-substitution records, off-diagonal covariance blocks) from
+ * the fixed array below instead of from cudaMalloc.  The caller still owns and
+ * passes the input and output arrays.
+ *
+ * The array is KALMAN_GPU_NOALLOC_SCRATCH_BYTES (64 MiB) on every device that
+ * loads the library, for the life of the process.  In host code its name is
+ * only a host-side stand-in, so its device address is looked up with
+ * cudaGetSymbolAddress, once per device, by the first call made with that
+ * device current; that first call should come before any stream capture.
+ * Every call shares the array and finds the previous call's contents in it;
+ * everything the kernels read is written first in the same call, except the
+ * status flag, which is cleared.  Host-side bookkeeping uses a fixed static
+ * table and a mutex, and each call waits for its kernels before returning, so
+ * calls through this entry point do not overlap; work that did overlap on the
+ * GPU with a call would race on the array.
+ * ------------------------------------------------------------------------ */
+static __device__ __align__(256) unsigned char g_noalloc_scratch[KALMAN_GPU_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr size_t kNoallocTabEntries = size_t(1) << 16; /* host plan tables, int64 entries */
+int64_t g_noalloc_tab[kNoallocTabEntries];
+std::mutex g_noalloc_mutex;
+constexpr int kNoallocDevices = 64;
+void* g_noalloc_addr[kNoallocDevices] = {nullptr};
+}  // namespace
+
+extern "C" int kalman_gpu_smooth_oddeven_noalloc(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream)
+{
+  ukg_clear_error();
+  if (int e = ukg_validate_problem(p, 0)) return e;
+  if (p->location != KALMAN_GPU_DEVICE)
+    return ukg_set_error(KALMAN_GPU_EINVAL, "the allocation-free entry point takes device arrays only "
+                         "(host arrays would need a device copy)");
+  if (p->nsteps == 0) return 0;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) {
+    cudaGetLastError();
+    return ukg_set_error(KALMAN_GPU_ENODEV, "no CUDA device: %s", cudaGetErrorString(ce));
+  }
+  if (dev < 0 || dev >= kNoallocDevices) return ukg_set_error(KALMAN_GPU_EINVAL, "device index %d too large", dev);
+  if (!g_noalloc_addr[dev]) { /* set-up, once per device, with that device current */
+    void* ptr = nullptr;
+    ce = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (ce != cudaSuccess || !ptr) {
+      cudaGetLastError();
+      return ukg_set_error(KALMAN_GPU_ECUDA, "cudaGetSymbolAddress of the scratch array failed: %s",
+                           cudaGetErrorString(ce));
+    }
+    g_noalloc_addr[dev] = ptr;
+  }
+  const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
+  Plan P;
+  const size_t need = build_plan(p, want_cov, P, nullptr, 0);
+  if (need == 0 || need > kNoallocTabEntries)
+    return ukg_set_error(KALMAN_GPU_EINVAL, "the allocation-free entry point plans at most %zu table entries "
+                         "(this problem needs %zu: too many tracks)", kNoallocTabEntries, need);
+  build_plan(p, want_cov, P, g_noalloc_tab, kNoallocTabEntries);
+  if (P.bytes > (size_t)KALMAN_GPU_NOALLOC_SCRATCH_BYTES)
+    return ukg_set_error(KALMAN_GPU_EINVAL, "this problem needs %zu bytes of scratch; the allocation-free entry "
+                         "point has %zu (use kalman_gpu_smooth_oddeven_packed)", P.bytes,
+                         (size_t)KALMAN_GPU_NOALLOC_SCRATCH_BYTES);
+  const int prof = ukg_prof_pause(); /* profiling would create CUDA events */
+  const int status = run_plan(options, p, (cudaStream_t)cuda_stream, P, g_noalloc_tab, (char*)g_noalloc_addr[dev]);
+  ukg_prof_resume(prof);
+  return status;
 }

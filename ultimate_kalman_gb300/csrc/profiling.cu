@@ -81,6 +81,15 @@ void ukg_prof_collect(void)
   cudaGetLastError();
 }
 
+int ukg_prof_pause(void)
+{
+  const int was = tl.on ? 1 : 0;
+  tl.on = false;
+  return was;
+}
+
+void ukg_prof_resume(int previous) { tl.on = previous != 0; }
+
 extern "C" void kalman_gpu_profile_enable(int on)
 {
   tl.on = on != 0;

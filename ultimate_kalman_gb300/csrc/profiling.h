@@ -21,6 +21,9 @@ enum {
 void ukg_prof_before(cudaStream_t st, int kind, cudaEvent_t* mark);
 void ukg_prof_after(cudaStream_t st, int kind, cudaEvent_t mark);
 void ukg_prof_collect(void);
+/* turns event timing off for the calling thread; returns the previous state */
+int  ukg_prof_pause(void);
+void ukg_prof_resume(int previous);
 
 /* brackets one kernel launch statement */
 #define UKG_LAUNCH(kind, stream, launch)              \

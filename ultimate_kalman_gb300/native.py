@@ -84,7 +84,7 @@ EXPORTED = [
     "kalman_gpu_last_status", "kalman_gpu_last_error", "kalman_gpu_clear_error",
     "kalman_gpu_smooth_oddeven_packed", "kalman_gpu_smooth_associative_packed", "kalman_gpu_smooth_tracks",
     "kalman_gpu_release", "kalman_gpu_profile_enable", "kalman_gpu_profile_read", "kalman_gpu_launch_count",
-    "kalman_gpu_measure_fp64_tflops",
+    "kalman_gpu_measure_fp64_tflops", "kalman_gpu_smooth_oddeven_noalloc",
 ]
 
 _lib = None
@@ -99,7 +99,8 @@ def load(path=LIB_PATH):
         raise FileNotFoundError(f"{path} is missing: run ultimate_kalman_gb300/build.py (or __graft_entry__.build())")
     L = ctypes.CDLL(path)
     P = ctypes.POINTER(ProblemStruct)
-    for f in ("kalman_gpu_smooth_oddeven_packed", "kalman_gpu_smooth_associative_packed"):
+    for f in ("kalman_gpu_smooth_oddeven_packed", "kalman_gpu_smooth_associative_packed",
+              "kalman_gpu_smooth_oddeven_noalloc"):
         getattr(L, f).argtypes = [ctypes.c_uint32, P, ctypes.c_void_p]
         getattr(L, f).restype = ctypes.c_int
     L.kalman_gpu_last_error.restype = ctypes.c_char_p
