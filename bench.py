@@ -1,27 +1,32 @@
 #!/usr/bin/env python3
 """Benchmark: batched odd-even Kalman smoothing on GB300 (smoothed steps/s).
 
-Workload (default, "batched"): 4,096 independent constant-velocity tracks
-(n=6 [pos; vel], m=3, dt=0.1, process noise diag(1e-2), observation noise
-diag(1e-1), prior N(0, I) folded into a square step-0 observation), lengths
-floor(exp(U[ln 100, ln 20000])) from a fixed seed -- 15.1 million steps,
-23.3 GB of FP64 equations (larger than the 126 MB L2, so nothing is re-read
-from cache between timed steps).  Data is synthetic (seeded NumPy).
+Workload: 4,096 independent constant-velocity tracks (n=6 [pos; vel], m=3,
+dt=0.1, process noise diag(1e-2), observation noise diag(1e-1), prior N(0, I)
+folded into a square step-0 observation), lengths floor(exp(U[ln 100,
+ln 20000])) from a fixed seed -- 15.1 million steps, 23.3 GB of FP64
+equations (larger than the 126 MB L2, so nothing is re-read from cache
+between timed steps).  Data is synthetic (seeded NumPy).
 
-One "step" of the benchmark = one full odd-even smoothing (states and
-covariances, FP64) of every track, through the library's C ABI:
+One "step" of the benchmark = one odd-even smoothing of every track through
+the library's C ABI.  The headline is the precision form: FP32 factorization
+with FP64-residual refinement of the smoothed states (KALMAN_GPU_FP32_REFINE),
+whose error against the plain FP64 path is measured in the same run and must
+be <= 1e-9; the plain FP64 path (states, and states + covariances) is timed
+beside it.
   value -- inputs resident in HBM, kalman_gpu_smooth_oddeven_packed on device
            arrays (CUDA events on the launching stream, synchronized);
   e2e   -- the same call handed page-locked HOST arrays: host->device copy of
-           the equations, smoothing, device->host copy of states and
-           covariances all inside the timed region.
-Other keys: per-kernel roofline (FP64 pipe: the kernels are arithmetic-bound),
-CPU baseline (the oracle's C restatement of the reference
-smoother on all host cores, a bounded sample of the same tracks), clocks.
+           the equations, smoothing, device->host copy of the states inside
+           the timed region.
+Other keys: per-kernel roofline, p50/p99 per-smoothing latency, the CPU
+baseline (the oracle's C restatement of the reference smoother, states only as
+the headline computes, on all host cores, a bounded sample of the same
+tracks), clocks.
 
 --impl reference: times the CPU restatement of the reference's odd-even
-smoother (oracle/kalman_oracle.c, OpenMP over tracks) on a bounded sample of
-the same workload, per step, with all host threads.
+smoother (oracle/kalman_oracle.c, OpenMP over tracks, FP64, states only) on a
+bounded sample of the same workload, per step, with all host threads.
 
 Multi-GPU (torchrun): every rank smooths its own 4,096 tracks (different
 seed); no collective on the data path (replicas); value = all ranks' steps /
@@ -42,7 +47,7 @@ import numpy as np
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
-METRIC = "smoothed steps/s (batched odd-even, FP64)"
+METRIC = "smoothed steps/s (batched odd-even), FP32 factorization + FP64-residual refinement vs plain FP64, at <=1e-9 rel err"
 UNIT = "steps/s"
 
 
@@ -57,6 +62,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--sweeps", type=int, default=0, help="refinement sweeps (0: library default)")
     return ap.parse_args()
 
 
@@ -74,9 +80,10 @@ def workload(tracks, rank):
 
 
 def config_dict(P, tracks, world):
-    return {"workload": "batched constant-velocity tracks, odd-even smoother (states + covariances)",
+    return {"workload": "batched constant-velocity tracks, odd-even smoother, smoothed states",
             "tracks_per_gpu": tracks, "steps_per_gpu": int(P.nsteps), "n": 6, "m": 3,
-            "track_lengths": "floor(exp(U[ln 100, ln 20000]))", "precision": "FP64",
+            "track_lengths": "floor(exp(U[ln 100, ln 20000]))",
+            "precision": "FP32 factorization + FP64-residual refinement (plain FP64 timed beside it)",
             "l2": "inputs (23 GB/GPU) exceed L2; no flush needed", "parallelism": f"replicas x{world}"}
 
 
@@ -115,19 +122,20 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_sample(P, seconds, threads=0, algorithm="oddeven"):
+def cpu_sample(P, seconds, threads=0, algorithm="oddeven", covariance=False):
     """Times the oracle's restatement on the first tracks of P, grown until the
-    sample takes about `seconds`; returns (steps/s, steps, tracks, threads)."""
+    sample takes about `seconds`; returns (steps/s, steps, tracks, threads,
+    seconds, states of the sample)."""
     import oracle
     nt = threads or oracle.max_threads()
     ntr = 8
     while True:
         S = P.select_tracks(range(min(ntr, P.ntracks)))
         t0 = time.perf_counter()
-        oracle.smooth(S, algorithm, covariance=True, threads=nt)
+        _, X, _ = oracle.smooth(S, algorithm, covariance=covariance, threads=nt)
         dt = time.perf_counter() - t0
         if dt >= seconds * 0.6 or ntr >= P.ntracks:
-            return S.nsteps / dt, S.nsteps, S.ntracks, nt, dt
+            return S.nsteps / dt, S.nsteps, S.ntracks, nt, dt, X
         ntr = min(P.ntracks, max(ntr * 2, int(ntr * seconds / max(dt, 1e-3))))
 
 
@@ -140,18 +148,18 @@ def run_reference(args):
     P = workload(args.tracks, 0)
     budget = max(1.0, 150.0 / max(1, args.steps + args.warmup))
     # choose the sample once, then time each step on it
-    _, _, ntr, nt, _ = cpu_sample(P, budget)
+    _, _, ntr, nt, _, _ = cpu_sample(P, budget)
     S = P.select_tracks(range(ntr))
     for _ in range(args.warmup):
-        oracle.smooth(S, "oddeven", threads=nt)
+        oracle.smooth(S, "oddeven", covariance=False, threads=nt)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        oracle.smooth(S, "oddeven", threads=nt)
+        oracle.smooth(S, "oddeven", covariance=False, threads=nt)
         times.append(time.perf_counter() - t0)
     ms = 1e3 * float(np.mean(times))
     v = S.nsteps / (ms * 1e-3)
-    sample = f"first {ntr} of {P.ntracks} tracks ({S.nsteps} steps) per step"
+    sample = f"first {ntr} of {P.ntracks} tracks ({S.nsteps} steps) per step, FP64 odd-even, states only"
     line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -159,6 +167,42 @@ def run_reference(args):
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": nt, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def time_smooths(D, steps, stream, **kw):
+    """Times `steps` smoothings, each bracketed by CUDA events on `stream`;
+    returns (mean ms, per-smoothing ms list)."""
+    import torch
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    torch.cuda.synchronize()
+    evs[0].record(stream)
+    for i in range(steps):
+        D.smooth("oddeven", stream=stream, **kw)
+        evs[i + 1].record(stream)
+    torch.cuda.synchronize()
+    per = [evs[i].elapsed_time(evs[i + 1]) for i in range(steps)]
+    return evs[0].elapsed_time(evs[-1]) / steps, per
+
+
+def roofline_for(prof, fl, steps, fp64_peak, fp32_peak, hbm_peak, bytes_model):
+    top = max(prof, key=lambda k: prof[k][0])
+    kms, kl = prof[top]
+    secs = kms * 1e-3 / steps
+    flops = fl.get(top, 0.0)
+    is32 = top.startswith("fp32") or top == "refine_kernel"
+    peak_f = fp32_peak if is32 else fp64_peak
+    ach_f = flops / secs / 1e12
+    ach_b = bytes_model.get(top, 0.0) / secs / 1e9
+    frac_f, frac_b = ach_f / peak_f, ach_b / hbm_peak
+    if frac_b > frac_f:
+        r = {"bound": "hbm", "achieved": ach_b, "peak": hbm_peak, "unit": "GB/s", "frac": frac_b,
+             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    else:
+        r = {"bound": "fp32" if is32 else "fp64", "achieved": ach_f, "peak": peak_f, "unit": "TFLOP/s",
+             "frac": frac_f, "peak_source": "FMA-chain probe kernel timed in this run (of measured)"}
+    r.update({"kernel": top, "traffic": None, "fp_tflops": ach_f, "fp_frac": frac_f, "hbm_gbs": ach_b,
+              "hbm_frac": frac_b, "flops_model": "ultimate_kalman_gb300/flops.py (FMA = 2 flops)"})
+    return r
 
 
 def run_gpu(args):
@@ -173,8 +217,9 @@ def run_gpu(args):
     native.load()
     P = workload(args.tracks, rank)
     D = native.DeviceProblem(P, covariance=True)
+    fp32 = dict(covariance=False, fp32_refine=True, sweeps=args.sweeps)
     for _ in range(args.warmup):
-        D.smooth("oddeven", covariance=True)
+        D.smooth("oddeven", **fp32)
     torch.cuda.synchronize()
 
     def barrier():
@@ -183,22 +228,16 @@ def run_gpu(args):
 
     sampler = ClockSampler(local)
     stream = torch.cuda.current_stream()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     native.profile_enable(True)
     launches0 = native.launch_count()
     barrier()
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    for _ in range(args.steps):
-        D.smooth("oddeven", covariance=True, stream=stream)
-    ev1.record(stream)
-    torch.cuda.synchronize()
+    ms, per = time_smooths(D, args.steps, stream, **fp32)
     barrier()
     launches = native.launch_count() - launches0
     prof = native.profile_read()
     native.profile_enable(False)
     clocks = sampler.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
+    X32 = D.state.clone()
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -206,39 +245,44 @@ def run_gpu(args):
     total_steps = P.nsteps * world
     value = total_steps / (ms * 1e-3)
 
-    # states-only throughput (KALMAN_NO_COVARIANCE), for reference
-    ev0.record(stream)
-    for _ in range(max(1, args.steps // 2)):
-        D.smooth("oddeven", covariance=False, stream=stream)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    ms_nocov = ev0.elapsed_time(ev1) / max(1, args.steps // 2)
+    # the plain FP64 path: states + covariances, and states only
+    D.smooth("oddeven", covariance=True)
+    native.profile_enable(True)
+    ms64c, _ = time_smooths(D, max(2, args.steps // 2), stream, covariance=True)
+    prof64 = native.profile_read()
+    native.profile_enable(False)
+    ms64, _ = time_smooths(D, max(2, args.steps // 2), stream, covariance=False)
+    X64 = D.state
+    err = float(((X32 - X64).abs().amax(dim=1) / X64.abs().amax(dim=1)).max().item())
 
-    # roofline of the dominant kernel: FP64 pipe
-    fl = flops.plan_flops_fast(P.track_lengths(), 6, 3, covariance=True)
-    top = max(prof, key=lambda k: prof[k][0])
-    kms, kl = prof[top]
-    achieved = fl[top] * args.steps / (kms * 1e-3) / 1e12
-    peak = native.measure_fp64_tflops(32)
-    total_tf = sum(fl.values()) / (ms * 1e-3) / 1e12
-    per_kernel = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps,
-                      "share": v[0] / sum(x[0] for x in prof.values()),
-                      "tflops": fl.get(k, 0.0) * args.steps / (v[0] * 1e-3) / 1e12} for k, v in prof.items()}
-    traffic = None
+    peak64 = native.measure_fp64_tflops(32)
+    peak32 = native.measure_fp32_tflops()
+    peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(REPO, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
+    fl32 = flops.plan_flops_fast_fp32(P.track_lengths(), 6, 3, sweeps=args.sweeps or 2)
+    fl64 = flops.plan_flops_fast(P.track_lengths(), 6, 3, covariance=True)
+    by32 = flops.plan_bytes_fast(P.track_lengths(), 6, 6, fp32=True, sweeps=args.sweeps or 2)
+    by64 = flops.plan_bytes_fast(P.track_lengths(), 6, 6, fp32=False)
+    roof = roofline_for(prof, fl32, args.steps, peak64, peak32, peaks["hbm_gbs"], by32)
     tfile = os.path.join(REPO, "profiles", "traffic_per_launch.json")
     if os.path.exists(tfile):
-        traffic = json.load(open(tfile)).get(top)
-    roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": top,
-                "peak_source": "FP64 FMA-chain probe kernel timed in this run (MEASURED_PEAKS.json has no FP64 figure)",
-                "flops_model": "ultimate_kalman_gb300/flops.py (FMA = 2 flops)",
-                "whole_smoother_tflops": total_tf, "per_kernel": per_kernel}
+        roof["traffic"] = json.load(open(tfile)).get(roof["kernel"])
+    roof["per_kernel"] = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps,
+                              "share": v[0] / sum(x[0] for x in prof.values())} for k, v in prof.items()}
+    roof64 = roofline_for(prof64, fl64, max(2, args.steps // 2), peak64, peak32, peaks["hbm_gbs"], by64)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_dict(P, args.tracks, world),
-            "gpu_launches": int(launches), "roofline": roofline, "clocks": clocks,
-            "states_only": {"value": total_steps / (ms_nocov * 1e-3), "unit": UNIT, "ms_per_step": ms_nocov}}
+            "vs_baseline": None, "dtype": "f32 factorization + f64 residual refinement", "data": "synthetic",
+            "config": config_dict(P, args.tracks, world), "gpu_launches": int(launches),
+            "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
+                           "what": "one smoothing of all 4,096 tracks"},
+            "rel_err_vs_fp64": err, "roofline": roof, "clocks": clocks,
+            "plain_fp64": {"states_and_covariances": total_steps / (ms64c * 1e-3),
+                           "states_only": total_steps / (ms64 * 1e-3), "unit": UNIT,
+                           "speedup_fp32_refine_vs_fp64_states_only": ms64 / ms,
+                           "speedup_fp32_refine_vs_fp64_with_covariances": ms64c / ms, "roofline": roof64},
+            "peaks": {"fp64_tflops": peak64, "fp32_tflops": peak32, "hbm_gbs": peaks["hbm_gbs"]}}
 
     # end to end through the C ABI with page-locked host buffers
     if not args.no_e2e:
@@ -246,27 +290,28 @@ def run_gpu(args):
         torch.cuda.empty_cache()
         pin = {f: torch.from_numpy(np.ascontiguousarray(getattr(P, f))).pin_memory() for f in native._FIELDS}
         st_h = torch.empty((P.nsteps, 6), dtype=torch.float64).pin_memory()
-        cov_h = torch.empty((P.nsteps, 6, 6), dtype=torch.float64).pin_memory()
-        s = native.host_struct_from_tensors(P, pin, st_h, cov_h)
-        native.smooth_struct("oddeven", s, covariance=True)  # warm-up (device staging allocated)
+        s = native.host_struct_from_tensors(P, pin, st_h, None)
+        native.smooth_struct("oddeven", s, **fp32)  # warm-up (device staging allocated)
         times = []
         for _ in range(args.e2e_steps):
             barrier()
             t0 = time.perf_counter()
-            native.smooth_struct("oddeven", s, covariance=True)
+            native.smooth_struct("oddeven", s, **fp32)
             times.append(time.perf_counter() - t0)
-        e2e_ms = 1e3 * max(times) if world == 1 else 1e3 * float(np.mean(times))
+        e2e_ms = 1e3 * float(np.median(times))
         h2d = sum(t.numel() * t.element_size() for t in pin.values())
-        d2h = st_h.numel() * 8 + cov_h.numel() * 8
         line["e2e"] = {"value": total_steps / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                       "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
-                       "path": "kalman_gpu_smooth_oddeven_packed with KALMAN_GPU_HOST arrays"}
+                       "d2h_bytes_per_step": int(st_h.numel() * 8), "ms_per_step": e2e_ms,
+                       "path": "kalman_gpu_smooth_oddeven_packed, KALMAN_GPU_HOST arrays, FP32 + refinement"}
 
     if rank == 0 and world == 1 and not args.no_cpu:
-        v, nsteps, ntr, nt, dt = cpu_sample(P, args.cpu_seconds)
+        v, nsteps, ntr, nt, dt, Xo = cpu_sample(P, args.cpu_seconds)
+        Xg = X32[:nsteps].cpu().numpy()
+        err_o = float((np.abs(Xg - Xo).max(axis=1) / np.abs(Xo).max(axis=1)).max())
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nt, "kind": "port",
                                 "sample": f"first {ntr} of {P.ntracks} tracks ({nsteps} steps), {dt:.1f} s, "
-                                          f"oracle/kalman_oracle.c odd-even, OpenMP over tracks"}
+                                          f"oracle/kalman_oracle.c odd-even, FP64, states only, OpenMP over tracks",
+                                "rel_err_of_gpu_states_on_sample": err_o}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -55,6 +55,9 @@ enum {
 /* Option bit added to kalman_options_t: factor in FP32 and refine the
  * estimates with FP64 residuals of the least-squares system.                 */
 #define KALMAN_GPU_FP32_REFINE (1u << 20)
+/* Number of refinement sweeps with KALMAN_GPU_FP32_REFINE (1..3; 0 selects the
+ * default, 2).  Each sweep multiplies the error by about eps32 * cond(A)^2.  */
+#define KALMAN_GPU_REFINE_SWEEPS(k) (((uint32_t)(k) & 3u) << 21)
 
 /* Last error of the calling thread: status code and a one-line message.     */
 int         kalman_gpu_last_status(void);
@@ -116,6 +119,8 @@ int64_t kalman_gpu_launch_count(void);
  * TFLOP/s, with `active_lanes` (1..32) active threads per warp.  A diagnostic
  * for roofline reporting; takes a few milliseconds.                          */
 double  kalman_gpu_measure_fp64_tflops(int active_lanes);
+/* The same for FP32 fused multiply-adds (all lanes active).                 */
+double  kalman_gpu_measure_fp32_tflops(void);
 
 /* Allocation-free odd-even smoothing of a packed problem held in DEVICE
  * memory.  No counterpart in the reference: it exists for callers that must

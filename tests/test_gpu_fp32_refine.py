@@ -1,0 +1,58 @@
+"""The precision form of the odd-even smoother (KALMAN_GPU_FP32_REFINE): FP32
+factorization, FP64 residuals of the weighted least-squares system and two
+refinement sweeps with the FP32 factors.
+
+Bars: smoothed states within 1e-9 relative error of the FP64 oracle (the
+target of this form); covariances, computed from the FP32 factors, within
+1e-4 (FP32 accuracy)."""
+import numpy as np
+import pytest
+
+import oracle
+from ultimate_kalman_gb300 import native, problem as pb
+
+pytestmark = pytest.mark.gpu
+TOL_STATE = 1e-9
+TOL_COV32 = 1e-4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    native.load()
+
+
+def run(P, cov=False):
+    return native.smooth(P, "oddeven", covariance=cov, fp32_refine=True)
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5, 7, 8, 16, 17, 33, 100, 257])
+def test_lengths(k):
+    P = pb.constant_velocity([k], seed=k)
+    X, _ = run(P)
+    st, Xo, _ = oracle.smooth(P, "oddeven", covariance=False)
+    assert oracle.rel_err_states(X, Xo) < TOL_STATE
+
+
+@pytest.mark.parametrize("n,m,cov", [(2, 1, "C"), (4, 2, "W"), (5, 3, "w"), (6, 3, "F"), (8, 4, "C")])
+def test_shapes_missing(n, m, cov):
+    P = pb.random_dynamics([14, 6, 1, 9, 2], n, m, seed=n + 10 * m, K_type=cov, C_type=cov, missing=0.25,
+                           per_step=True)
+    X, S = run(P, cov=True)
+    st, Xo, So = oracle.smooth(P, "oddeven")
+    assert oracle.rel_err_states(X, Xo) < TOL_STATE
+    assert oracle.rel_err_covs(S, So) < TOL_COV32
+
+
+def test_batched_and_full_size():
+    lens = pb.batched_lengths(200, 50, 3000, seed=8)
+    P = pb.constant_velocity(lens, seed=9, missing=0.05)
+    X, _ = run(P)
+    st, Xo, _ = oracle.smooth(P, "oddeven", covariance=False)
+    assert oracle.rel_err_states(X, Xo) < TOL_STATE
+    P = pb.constant_velocity([100000], seed=10)
+    X, _ = run(P)
+    st, Xo, _ = oracle.smooth(P, "oddeven", covariance=False)
+    assert oracle.rel_err_states(X, Xo) < TOL_STATE

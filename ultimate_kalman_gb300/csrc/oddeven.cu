@@ -1,10 +1,10 @@
 /*
  * oddeven.cu -- the odd-even (Gargir-Toledo) parallel Kalman smoother on the
- * GPU, FP64.  Restates, as CUDA kernels, c/kalman_oddeven_smoother.c of
+ * GPU.  Restates, as CUDA kernels, c/kalman_oddeven_smoother.c of
  * UltimateKalman 2.1.0:
  *
  *   weigh_kernel     steps_weigh 1620-1659 + kalman_covariance_matrix_weigh
- *                    (c/kalman_base.c:61-175): V H, -V F, V c, W G, W o
+ *                    (c/kalman_base.c:61-175): V H, -V F, V c, W G, W o (FP64)
  *   pair_kernel      one thread per step pair (j, j+1) of a level:
  *                      stage A  G_F_to_R_tilde 379-457      QR of [G_j; F_{j+1}]
  *                      stage C  H_tilde_G_to_G_tilde 526-560 QR of [H~_{j+1}; G_{j+1}]
@@ -25,15 +25,27 @@
  * streamed column in shared memory, interleaved across the threads of the block
  * (element e of thread t at smem[e*blockDim + t]) so that accesses never
  * conflict.  Intermediate blocks travel through global memory in the record and
- * next-level arrays they end up in.
+ * next-level arrays they end up in.  Divisions are by reciprocals computed once
+ * per pivot: FP64 division and square root are multi-instruction sequences on
+ * the FP64 pipe, the resource these kernels are bound by.
  *
- * Layout in HBM (all FP64, "slot" = a step of a level, every track's slots start
- * at an even slot so pairs never straddle tracks):
+ * Precision.  The kernels are templates over the arithmetic type T.  FP64 is
+ * the plain path.  With KALMAN_GPU_FP32_REFINE the factorization (levels,
+ * records) is FP32, reading the FP64-weighed level-0 equations; the states are
+ * then refined with corrected semi-normal equations: the residual r = b - A x
+ * of the weighted block-bidiagonal least-squares system and z = A^T r in FP64
+ * (residual_kernel), R^T y = z level by level (rt_even_kernel, rt_odd_kernel,
+ * rt_base_kernel) and R d = y (solve_kernel with right-hand side y) with the
+ * FP32 R factors, x += d in FP64 -- one or two sweeps.
+ *
+ * Layout in HBM ("slot" = a step of a level, every track's slots start at an
+ * even slot so pairs never straddle tracks):
  *   level equations  F, H [n*n][S], c [n][S], G [mx*n][S], o [mx][S], m [S]
  *                    -- element-major ("SoA"): consecutive threads read
  *                    consecutive slots, so every load and store is coalesced
- *   records          R, Ft, Y [n*n][E], cr [n][E]: R x_j + Ft x_{j-1} + Y x_{j+1} = cr
+ *   records          R, Ft, Y [n*n][E], rhs [n][E]: R x_j + Ft x_{j-1} + Y x_{j+1} = rhs
  *   off-diagonals    U [n*n][S]: U[q] = cov(x_{q-1}, x_q) of the level
+ *   base factors     baseR [n*n][tracks] (refinement only)
  *   outputs          state [nsteps][n], covariance [nsteps][n*n] (caller's layout)
  * Level l slot q of track t is original step track_start[t] + ((q+1) << l) - 1.
  */
@@ -54,34 +66,60 @@ namespace {
 /* ---------------------------------------------------------------------------
  * per-thread views into interleaved shared memory
  * ------------------------------------------------------------------------ */
+template <typename T>
 struct PV {
-  double* p;
+  T* p;
   int s;
-  __device__ __forceinline__ double& operator[](int i) const { return p[i * s]; }
+  __device__ __forceinline__ T& operator[](int i) const { return p[i * s]; }
   __device__ __forceinline__ PV operator+(int off) const { return PV{p + off * s, s}; }
+};
+
+/* The same view with the stride (the block size) known at compile time, so
+ * that every shared-memory address is a base plus an immediate offset.       */
+template <typename T, int BS>
+struct PVc {
+  T* p;
+  __device__ __forceinline__ T& operator[](int i) const { return p[i * BS]; }
+  __device__ __forceinline__ PVc operator+(int off) const { return PVc{p + off * BS}; }
+};
+
+template <typename T, int BS>
+struct ViewOf {
+  using type = PVc<T, BS>;
+  static __device__ __forceinline__ type make(T* smem) { return type{smem + threadIdx.x}; }
+};
+template <typename T>
+struct ViewOf<T, 0> {
+  using type = PV<T>;
+  static __device__ __forceinline__ type make(T* smem) { return type{smem + threadIdx.x, (int)blockDim.x}; }
 };
 
 /* Householder triangularization of the rows x cols block W (leading dimension
  * ld) using the first npiv columns as pivots; reflector scalars go to tau
- * (tau[k] = 0 for an identity reflector).                                    */
-__device__ void householder(PV W, int ld, int rows, int npiv, int cols, PV tau)
+ * (tau[k] = 0 for an identity reflector).  One division per reflector: with
+ * inv = 1/(beta (alpha - beta)), 1/(alpha - beta) = beta inv and
+ * tau = (beta - alpha)/beta = -(alpha - beta)^2 inv.                        */
+template <typename T, class V>
+__device__ void householder(V W, int ld, int rows, int npiv, int cols, V tau)
 {
   const int nref = rows < npiv ? rows : npiv;
   for (int k = 0; k < nref; ++k) {
-    PV v = W + k * ld;
-    const double alpha = v[k];
-    double tail = 0.0;
+    V v = W + k * ld;
+    const T alpha = v[k];
+    T tail = T(0);
     for (int i = k + 1; i < rows; ++i) tail = fma(v[i], v[i], tail);
-    double t = 0.0;
-    if (tail != 0.0) {
-      const double beta = -copysign(sqrt(fma(alpha, alpha, tail)), alpha);
-      t = (beta - alpha) / beta;
-      const double scale = 1.0 / (alpha - beta);
+    T t = T(0);
+    if (tail != T(0)) {
+      const T beta = -copysign(sqrt(fma(alpha, alpha, tail)), alpha);
+      const T amb = alpha - beta;
+      const T inv = T(1) / (beta * amb);
+      t = -(amb * amb) * inv;
+      const T scale = beta * inv;
       for (int i = k + 1; i < rows; ++i) v[i] *= scale;
       v[k] = beta;
       for (int j = k + 1; j < cols; ++j) {
-        PV a = W + j * ld;
-        double d = a[k];
+        V a = W + j * ld;
+        T d = a[k];
         for (int i = k + 1; i < rows; ++i) d = fma(v[i], a[i], d);
         d *= t;
         a[k] -= d;
@@ -90,18 +128,19 @@ __device__ void householder(PV W, int ld, int rows, int npiv, int cols, PV tau)
     }
     tau[k] = t;
   }
-  for (int k = nref; k < npiv; ++k) tau[k] = 0.0;
+  for (int k = nref; k < npiv; ++k) tau[k] = T(0);
 }
 
 /* col <- Q^T col for the reflectors stored in W / tau by householder().      */
-__device__ void apply_qt(PV W, int ld, int rows, int npiv, PV tau, PV col)
+template <typename T, class V>
+__device__ void apply_qt(V W, int ld, int rows, int npiv, V tau, V col)
 {
   const int nref = rows < npiv ? rows : npiv;
   for (int k = 0; k < nref; ++k) {
-    const double t = tau[k];
-    if (t == 0.0) continue;
-    PV v = W + k * ld;
-    double d = col[k];
+    const T t = tau[k];
+    if (t == T(0)) continue;
+    V v = W + k * ld;
+    T d = col[k];
     for (int i = k + 1; i < rows; ++i) d = fma(v[i], col[i], d);
     d *= t;
     col[k] -= d;
@@ -109,33 +148,38 @@ __device__ void apply_qt(PV W, int ld, int rows, int npiv, PV tau, PV col)
   }
 }
 
-/* x <- U^{-1} x, U upper triangular n x n given by an element accessor.       */
-template <class UA, class XA>
-__device__ bool solve_upper(const UA& U, int n, XA& x)
+/* x <- U^{-1} x for the upper triangle of U (n x n) with precomputed
+ * reciprocals dinv of its diagonal.                                          */
+template <class UA, class DA, class XA>
+__device__ void solve_upper(const UA& U, const DA& dinv, int n, XA& x)
 {
-  bool bad = false;
   for (int j = n - 1; j >= 0; --j) {
-    const double d = U(j, j);
-    bad |= (d == 0.0);
-    const double xj = x(j) / d;
+    const auto xj = x(j) * dinv(j);
     x(j) = xj;
     for (int i = 0; i < j; ++i) x(i) = fma(-xj, U(i, j), x(i));
   }
-  return bad;
+}
+
+/* x <- U^{-T} x (forward substitution with the transpose of the upper U)     */
+template <class UA, class DA, class XA>
+__device__ void solve_upper_t(const UA& U, const DA& dinv, int n, XA& x)
+{
+  for (int i = 0; i < n; ++i) {
+    auto s = x(i);
+    for (int k = 0; k < i; ++k) s = fma(-U(k, i), x(k), s);
+    x(i) = s * dinv(i);
+  }
 }
 
 /* element-major (SoA) array: element e of slot s at p[e*stride + s]           */
+template <typename T>
 struct Soa {
-  double* p;
+  T* p;
   int64_t stride;
-  __device__ __forceinline__ double& at(int e, int64_t s) const { return p[(int64_t)e * stride + s]; }
+  __device__ __forceinline__ T& at(int e, int64_t s) const { return p[(int64_t)e * stride + s]; }
 };
 
-struct LevelDev {
-  Soa F, H, c, G, o;
-  int32_t* m;
-  Soa R, Ft, Y, cr;
-  Soa U;
+struct Tables {
   const int64_t* L;      /* [T] steps of each track at this level            */
   const int64_t* slot;   /* [T] first slot                                   */
   const int64_t* pair;   /* [T+1] prefix of floor(L/2) (tracks with L >= 2)  */
@@ -144,13 +188,30 @@ struct LevelDev {
   int64_t npairs, nsolve, ntail;
 };
 
+template <typename T>
+struct Eq {
+  Soa<T> F, H, c, G, o;
+  int32_t* m;
+};
+
+template <typename T>
+struct Rec {
+  Soa<T> R, Ft, Y, rhs, U;
+};
+
+template <typename T, typename TI>
 struct Args {
-  LevelDev cur, nxt;
+  Tables ct, nt;   /* current and next level                                  */
+  Eq<TI> ce;       /* equations of the current level                           */
+  Eq<T> ne;        /* equations of the next level                              */
+  Rec<T> cr, nr;   /* records and off-diagonal blocks, current / next level   */
   int n, mx, level, ntracks;
   const int64_t* track_start; /* device copy, [T+1] */
-  double* state;
+  double* state;   /* x, or the correction d in a refinement sweep            */
   double* cov;
   int* flag;
+  Soa<T> baseR;    /* base-case R per track (refinement), p may be null      */
+  Soa<T> yrhs;     /* refinement: right-hand side of the even steps          */
 };
 
 /* last t with base[t] <= i (base has T+1 nondecreasing entries, i < base[T]) */
@@ -164,13 +225,13 @@ __device__ __forceinline__ int find_track(const int64_t* base, int T, int64_t i)
   return lo;
 }
 
-__device__ __forceinline__ int64_t orig_step(const Args& a, int t, int64_t q)
+__device__ __forceinline__ int64_t orig_step(const int64_t* track_start, int level, int t, int64_t q)
 {
-  return a.track_start[t] + ((q + 1) << a.level) - 1;
+  return track_start[t] + ((q + 1) << level) - 1;
 }
 
 /* ---------------------------------------------------------------------------
- * level 0: weigh the raw equations into the SoA level arrays
+ * level 0: weigh the raw equations into the SoA level arrays (FP64)
  * ------------------------------------------------------------------------ */
 struct RawDev {
   const double *H, *F, *c, *K, *G, *o, *C;
@@ -181,26 +242,27 @@ struct RawDev {
 
 /* Weighs column `col` (rows entries) in place by the covariance factor
  * (cov, type, ld): 'W' cov*col, 'w' diag(cov)*col, 'C' chol(cov)^{-1} col,
- * 'U'/'F' tril(cov)^{-1} col.  L holds the prepared factor for 'C' (rows x rows
- * in shared memory, ld rows).  tmp has `rows` entries.                       */
-__device__ void weigh_column(char type, const double* cov, int ldc, int rows, PV L, PV col, PV tmp)
+ * 'U'/'F' tril(cov)^{-1} col.  L holds the lower factor for 'C' and 'U'/'F'
+ * (rows x rows, ld rows) and dinv the reciprocals of its diagonal; tmp has
+ * `rows` entries.  Arithmetic in T; the factors are read as FP64.             */
+template <typename T>
+__device__ void weigh_column(char type, const double* cov, int ldc, int rows, PV<T> L, PV<T> dinv, PV<T> col,
+                             PV<T> tmp)
 {
   if (type == 'W') {
     for (int i = 0; i < rows; ++i) {
-      double s = 0.0;
-      for (int j = 0; j < rows; ++j) s = fma(cov[(int64_t)j * ldc + i], col[j], s);
+      T s = T(0);
+      for (int j = 0; j < rows; ++j) s = fma((T)cov[(int64_t)j * ldc + i], col[j], s);
       tmp[i] = s;
     }
     for (int i = 0; i < rows; ++i) col[i] = tmp[i];
   } else if (type == 'w') {
-    for (int i = 0; i < rows; ++i) col[i] *= cov[i];
-  } else { /* forward substitution with a lower-triangular factor */
-    const bool c = (type == 'C');
+    for (int i = 0; i < rows; ++i) col[i] *= (T)cov[i];
+  } else { /* forward substitution with the lower-triangular factor */
     for (int j = 0; j < rows; ++j) {
-      const double d = c ? L[j * rows + j] : cov[(int64_t)j * ldc + j];
-      const double xj = col[j] / d;
+      const T xj = col[j] * dinv[j];
       col[j] = xj;
-      for (int i = j + 1; i < rows; ++i) col[i] = fma(-xj, c ? L[j * rows + i] : cov[(int64_t)j * ldc + i], col[i]);
+      for (int i = j + 1; i < rows; ++i) col[i] = fma(-xj, L[j * rows + i], col[i]);
     }
   }
 }
@@ -210,52 +272,69 @@ __device__ __forceinline__ bool valid_type(char c)
   return c == 'W' || c == 'w' || c == 'C' || c == 'U' || c == 'F';
 }
 
-/* lower Cholesky factor of cov (rows x rows) into L; false if not SPD        */
-__device__ bool cholesky(const double* cov, int ldc, int rows, PV L)
+/* the lower factor used by weigh_column: Cholesky of cov for 'C', the lower
+ * triangle of cov for 'U'/'F'; false if not positive definite / singular    */
+template <typename T>
+__device__ bool lower_factor(char type, const double* cov, int ldc, int rows, PV<T> L, PV<T> dinv)
 {
+  if (type == 'U' || type == 'F') {
+    bool ok = true;
+    for (int j = 0; j < rows; ++j) {
+      for (int i = j; i < rows; ++i) L[j * rows + i] = (T)cov[(int64_t)j * ldc + i];
+      const T d = L[j * rows + j];
+      ok &= (d != T(0));
+      dinv[j] = T(1) / d;
+    }
+    return ok;
+  }
+  if (type != 'C') return true;
   for (int j = 0; j < rows; ++j) {
-    double d = cov[(int64_t)j * ldc + j];
+    T d = (T)cov[(int64_t)j * ldc + j];
     for (int k = 0; k < j; ++k) d = fma(-L[k * rows + j], L[k * rows + j], d);
-    if (!(d > 0.0)) return false;
+    if (!(d > T(0))) return false;
     d = sqrt(d);
+    const T r = T(1) / d;
     L[j * rows + j] = d;
+    dinv[j] = r;
     for (int i = j + 1; i < rows; ++i) {
-      double s = cov[(int64_t)j * ldc + i];
+      T s = (T)cov[(int64_t)j * ldc + i];
       for (int k = 0; k < j; ++k) s = fma(-L[k * rows + i], L[k * rows + j], s);
-      L[j * rows + i] = s / d;
+      L[j * rows + i] = s * r;
     }
   }
   return true;
 }
 
-__global__ void weigh_kernel(Args a, RawDev raw, int64_t nsteps)
+template <typename T>
+__global__ void weigh_kernel(Args<T, T> a, RawDev raw, int64_t nsteps)
 {
-  extern __shared__ double smem[];
+  extern __shared__ unsigned char smem_raw[];
+  T* smem = reinterpret_cast<T*>(smem_raw);
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= nsteps) return;
   const int n = a.n, mx = a.mx, mm = raw.mmax;
-  PV ws{smem + threadIdx.x, (int)blockDim.x};
-  PV L = ws, col = ws + mx * mx, tmp = ws + mx * mx + mx;
+  PV<T> ws{smem + threadIdx.x, (int)blockDim.x};
+  PV<T> L = ws, dinv = ws + mx * mx, col = dinv + mx, tmp = col + mx;
   const int t = find_track(a.track_start, a.ntracks, g);
   const int64_t i = g - a.track_start[t];
-  const int64_t q = a.cur.slot[t] + i;
+  const int64_t q = a.ct.slot[t] + i;
   const int64_t nn = (int64_t)n * n;
   bool bad = false;
   if (i > 0) {
     const char kt = raw.K_type[g];
     if (!valid_type(kt)) atomicOr(a.flag, 4);
     const double* K = raw.K + g * nn;
-    if (kt == 'C') bad |= !cholesky(K, n, n, L);
+    bad |= !lower_factor(kt, K, n, n, L, dinv);
     for (int part = 0; part <= 2 * n; ++part) { /* n columns of H, n of F, then c */
       const double* src = part < n ? raw.H + g * nn + (int64_t)part * n
                         : part < 2 * n ? raw.F + g * nn + (int64_t)(part - n) * n : raw.c + g * n;
-      const double sgn = (part >= n && part < 2 * n) ? -1.0 : 1.0;
-      for (int r = 0; r < n; ++r) col[r] = sgn * src[r];
-      weigh_column(kt, K, n, n, L, col, tmp);
+      const T sgn = (part >= n && part < 2 * n) ? T(-1) : T(1);
+      for (int r = 0; r < n; ++r) col[r] = sgn * (T)src[r];
+      weigh_column(kt, K, n, n, L, dinv, col, tmp);
       for (int r = 0; r < n; ++r) {
-        if (part < n) a.cur.H.at(part * n + r, q) = col[r];
-        else if (part < 2 * n) a.cur.F.at((part - n) * n + r, q) = col[r];
-        else a.cur.c.at(r, q) = col[r];
+        if (part < n) a.ce.H.at(part * n + r, q) = col[r];
+        else if (part < 2 * n) a.ce.F.at((part - n) * n + r, q) = col[r];
+        else a.ce.c.at(r, q) = col[r];
       }
     }
   }
@@ -264,19 +343,19 @@ __global__ void weigh_kernel(Args a, RawDev raw, int64_t nsteps)
     m = 0;
     atomicOr(a.flag, 4);
   }
-  a.cur.m[q] = m;
+  a.ce.m[q] = m;
   if (m > 0) {
     const char ct = raw.C_type[g];
     if (!valid_type(ct)) atomicOr(a.flag, 4);
     const double* C = raw.C + g * (int64_t)mm * mm;
-    if (ct == 'C') bad |= !cholesky(C, mm, m, L);
+    bad |= !lower_factor(ct, C, mm, m, L, dinv);
     for (int part = 0; part <= n; ++part) { /* n columns of G, then o */
       const double* src = part < n ? raw.G + g * (int64_t)mm * n + (int64_t)part * mm : raw.o + g * mm;
-      for (int r = 0; r < m; ++r) col[r] = src[r];
-      weigh_column(ct, C, mm, m, L, col, tmp);
+      for (int r = 0; r < m; ++r) col[r] = (T)src[r];
+      weigh_column(ct, C, mm, m, L, dinv, col, tmp);
       for (int r = 0; r < m; ++r) {
-        if (part < n) a.cur.G.at(part * mx + r, q) = col[r];
-        else a.cur.o.at(r, q) = col[r];
+        if (part < n) a.ce.G.at(part * mx + r, q) = col[r];
+        else a.ce.o.at(r, q) = col[r];
       }
     }
   }
@@ -286,44 +365,50 @@ __global__ void weigh_kernel(Args a, RawDev raw, int64_t nsteps)
 /* ---------------------------------------------------------------------------
  * forward elimination of one pair of a level
  * ------------------------------------------------------------------------ */
-__global__ void pair_kernel(Args a, int rmax)
+/* NT, MT: compile-time n and mx (0: taken from the arguments); BS: the
+ * compile-time block size (0: runtime)                                      */
+template <typename T, typename TI, int NT = 0, int MT = 0, int BS = 0>
+__global__ void __launch_bounds__(BS ? BS : 1024) pair_kernel(Args<T, TI> a, int rmax_rt)
 {
-  extern __shared__ double smem[];
+  extern __shared__ unsigned char smem_raw[];
+  T* smem = reinterpret_cast<T*>(smem_raw);
   const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (item >= a.cur.npairs) return;
-  const int n = a.n, mx = a.mx;
-  PV ws{smem + threadIdx.x, (int)blockDim.x};
-  PV W = ws, tau = ws + rmax * (n + 1), col = tau + n;
+  if (item >= a.ct.npairs) return;
+  const int n = NT ? NT : a.n, mx = MT ? MT : a.mx, rmax = MT ? 2 * MT : rmax_rt;
+  using View = typename ViewOf<T, BS>::type;
+  View ws = ViewOf<T, BS>::make(smem);
+  View W = ws, tau = ws + rmax * (n + 1), col = tau + n;
 
-  const LevelDev& C = a.cur;
-  const LevelDev& N = a.nxt;
-  const int t = find_track(C.pair, a.ntracks, item);
-  const int64_t p = item - C.pair[t];
-  const int64_t sj = C.slot[t] + 2 * p, sj1 = sj + 1;
-  const int64_t sn = N.slot[t] + p;
-  const int64_t se = C.solve[t] + p;
+  const Eq<TI>& C = a.ce;
+  const Eq<T>& N = a.ne;
+  const Rec<T>& Rr = a.cr;
+  const int t = find_track(a.ct.pair, a.ntracks, item);
+  const int64_t p = item - a.ct.pair[t];
+  const int64_t sj = a.ct.slot[t] + 2 * p, sj1 = sj + 1;
+  const int64_t sn = a.nt.slot[t] + p;
+  const int64_t se = a.ct.solve[t] + p;
   const int mj = C.m[sj], mj1 = C.m[sj1];
 
   /* stage A: pivot [G_j; F_{j+1}], rhs [o_j; c_{j+1}] */
   {
     const int rA = mj + n, ld = rA;
     for (int q = 0; q < n; ++q) {
-      for (int i = 0; i < mj; ++i) W[q * ld + i] = C.G.at(q * mx + i, sj);
-      for (int i = 0; i < n; ++i) W[q * ld + mj + i] = C.F.at(q * n + i, sj1);
+      for (int i = 0; i < mj; ++i) W[q * ld + i] = (T)C.G.at(q * mx + i, sj);
+      for (int i = 0; i < n; ++i) W[q * ld + mj + i] = (T)C.F.at(q * n + i, sj1);
     }
-    for (int i = 0; i < mj; ++i) W[n * ld + i] = C.o.at(i, sj);
-    for (int i = 0; i < n; ++i) W[n * ld + mj + i] = C.c.at(i, sj1);
-    householder(W, ld, rA, n, n + 1, tau);
+    for (int i = 0; i < mj; ++i) W[n * ld + i] = (T)C.o.at(i, sj);
+    for (int i = 0; i < n; ++i) W[n * ld + mj + i] = (T)C.c.at(i, sj1);
+    householder<T>(W, ld, rA, n, n + 1, tau);
     for (int q = 0; q < n; ++q)
-      for (int i = 0; i < n; ++i) C.R.at(q * n + i, se) = (i <= q) ? W[q * ld + i] : 0.0;
-    for (int i = 0; i < n; ++i) C.cr.at(i, se) = W[n * ld + i];
+      for (int i = 0; i < n; ++i) Rr.R.at(q * n + i, se) = (i <= q) ? W[q * ld + i] : T(0);
+    for (int i = 0; i < n; ++i) Rr.rhs.at(i, se) = W[n * ld + i];
     for (int i = 0; i < mj; ++i) N.o.at(i, sn) = W[n * ld + n + i]; /* c'_{j+1} */
     /* stream [0; H_{j+1}]: X_j -> record Y (temporarily), H~_{j+1} -> next G */
     for (int q = 0; q < n; ++q) {
-      for (int i = 0; i < mj; ++i) col[i] = 0.0;
-      for (int i = 0; i < n; ++i) col[mj + i] = C.H.at(q * n + i, sj1);
-      apply_qt(W, ld, rA, n, tau, col);
-      for (int i = 0; i < n; ++i) C.Y.at(q * n + i, se) = col[i];
+      for (int i = 0; i < mj; ++i) col[i] = T(0);
+      for (int i = 0; i < n; ++i) col[mj + i] = (T)C.H.at(q * n + i, sj1);
+      apply_qt<T>(W, ld, rA, n, tau, col);
+      for (int i = 0; i < n; ++i) Rr.Y.at(q * n + i, se) = col[i];
       for (int i = 0; i < mj; ++i) N.G.at(q * mx + i, sn) = col[n + i];
     }
   }
@@ -333,50 +418,50 @@ __global__ void pair_kernel(Args a, int rmax)
     const int rC = mj + mj1, ld = rC > 0 ? rC : 1;
     for (int q = 0; q < n; ++q) {
       for (int i = 0; i < mj; ++i) W[q * ld + i] = N.G.at(q * mx + i, sn);
-      for (int i = 0; i < mj1; ++i) W[q * ld + mj + i] = C.G.at(q * mx + i, sj1);
+      for (int i = 0; i < mj1; ++i) W[q * ld + mj + i] = (T)C.G.at(q * mx + i, sj1);
     }
     for (int i = 0; i < mj; ++i) W[n * ld + i] = N.o.at(i, sn);
-    for (int i = 0; i < mj1; ++i) W[n * ld + mj + i] = C.o.at(i, sj1);
-    householder(W, ld, rC, n, n + 1, tau);
+    for (int i = 0; i < mj1; ++i) W[n * ld + mj + i] = (T)C.o.at(i, sj1);
+    householder<T>(W, ld, rC, n, n + 1, tau);
     const int g = rC < n ? rC : n;
     for (int q = 0; q < n; ++q)
-      for (int i = 0; i < g; ++i) N.G.at(q * mx + i, sn) = (i <= q) ? W[q * ld + i] : 0.0;
+      for (int i = 0; i < g; ++i) N.G.at(q * mx + i, sn) = (i <= q) ? W[q * ld + i] : T(0);
     for (int i = 0; i < g; ++i) N.o.at(i, sn) = W[n * ld + i];
     N.m[sn] = g;
   }
 
   /* stage B */
   if (p == 0) {
-    for (int e = 0; e < n * n; ++e) C.Ft.at(e, se) = 0.0;
+    for (int e = 0; e < n * n; ++e) Rr.Ft.at(e, se) = T(0);
     return;
   }
   {
     const int ld = 2 * n;
     for (int q = 0; q < n; ++q) {
-      for (int i = 0; i < n; ++i) W[q * ld + i] = C.H.at(q * n + i, sj);
-      for (int i = 0; i < n; ++i) W[q * ld + n + i] = C.R.at(q * n + i, se);
+      for (int i = 0; i < n; ++i) W[q * ld + i] = (T)C.H.at(q * n + i, sj);
+      for (int i = 0; i < n; ++i) W[q * ld + n + i] = Rr.R.at(q * n + i, se);
     }
-    for (int i = 0; i < n; ++i) W[n * ld + i] = C.c.at(i, sj);
-    for (int i = 0; i < n; ++i) W[n * ld + n + i] = C.cr.at(i, se);
-    householder(W, ld, 2 * n, n, n + 1, tau);
+    for (int i = 0; i < n; ++i) W[n * ld + i] = (T)C.c.at(i, sj);
+    for (int i = 0; i < n; ++i) W[n * ld + n + i] = Rr.rhs.at(i, se);
+    householder<T>(W, ld, 2 * n, n, n + 1, tau);
     for (int q = 0; q < n; ++q)
-      for (int i = 0; i < n; ++i) C.R.at(q * n + i, se) = (i <= q) ? W[q * ld + i] : 0.0;
-    for (int i = 0; i < n; ++i) C.cr.at(i, se) = W[n * ld + i];
+      for (int i = 0; i < n; ++i) Rr.R.at(q * n + i, se) = (i <= q) ? W[q * ld + i] : T(0);
+    for (int i = 0; i < n; ++i) Rr.rhs.at(i, se) = W[n * ld + i];
     for (int i = 0; i < n; ++i) N.c.at(i, sn) = W[n * ld + n + i];
     /* stream [F_j; 0] -> F~_j (record) and Z_j (next F) */
     for (int q = 0; q < n; ++q) {
-      for (int i = 0; i < n; ++i) col[i] = C.F.at(q * n + i, sj);
-      for (int i = 0; i < n; ++i) col[n + i] = 0.0;
-      apply_qt(W, ld, 2 * n, n, tau, col);
-      for (int i = 0; i < n; ++i) C.Ft.at(q * n + i, se) = col[i];
+      for (int i = 0; i < n; ++i) col[i] = (T)C.F.at(q * n + i, sj);
+      for (int i = 0; i < n; ++i) col[n + i] = T(0);
+      apply_qt<T>(W, ld, 2 * n, n, tau, col);
+      for (int i = 0; i < n; ++i) Rr.Ft.at(q * n + i, se) = col[i];
       for (int i = 0; i < n; ++i) N.F.at(q * n + i, sn) = col[n + i];
     }
     /* stream [0; X_j] -> Y_j (record) and X~_j (next H) */
     for (int q = 0; q < n; ++q) {
-      for (int i = 0; i < n; ++i) col[i] = 0.0;
-      for (int i = 0; i < n; ++i) col[n + i] = C.Y.at(q * n + i, se);
-      apply_qt(W, ld, 2 * n, n, tau, col);
-      for (int i = 0; i < n; ++i) C.Y.at(q * n + i, se) = col[i];
+      for (int i = 0; i < n; ++i) col[i] = T(0);
+      for (int i = 0; i < n; ++i) col[n + i] = Rr.Y.at(q * n + i, se);
+      apply_qt<T>(W, ld, 2 * n, n, tau, col);
+      for (int i = 0; i < n; ++i) Rr.Y.at(q * n + i, se) = col[i];
       for (int i = 0; i < n; ++i) N.H.at(q * n + i, sn) = col[n + i];
     }
   }
@@ -385,22 +470,25 @@ __global__ void pair_kernel(Args a, int rmax)
 /* ---------------------------------------------------------------------------
  * odd-length tracks: single last step + fix-up, or the one-step base case
  * ------------------------------------------------------------------------ */
-__global__ void tail_kernel(Args a)
+template <typename T, typename TI>
+__global__ void tail_kernel(Args<T, TI> a)
 {
-  extern __shared__ double smem[];
+  extern __shared__ unsigned char smem_raw[];
+  T* smem = reinterpret_cast<T*>(smem_raw);
   const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (item >= a.cur.ntail) return;
+  if (item >= a.ct.ntail) return;
   const int n = a.n, mx = a.mx;
-  const LevelDev& C = a.cur;
-  const LevelDev& N = a.nxt;
-  PV ws{smem + threadIdx.x, (int)blockDim.x};
-  const int t = (int)C.tail[item];
-  const int64_t L = C.L[t];
-  const int64_t sb = C.slot[t];
+  const Eq<TI>& C = a.ce;
+  const Eq<T>& N = a.ne;
+  const Rec<T>& Rr = a.cr;
+  PV<T> ws{smem + threadIdx.x, (int)blockDim.x};
+  const int t = (int)a.ct.tail[item];
+  const int64_t L = a.ct.L[t];
+  const int64_t sb = a.ct.slot[t];
 
   if (L == 1) { /* base case: x = R^{-1} Q^T o, S = R^{-1} R^{-T} */
     const int m0 = C.m[sb];
-    const int64_t os = orig_step(a, t, 0);
+    const int64_t os = orig_step(a.track_start, a.level, t, 0);
     double* x = a.state + os * n;
     double* S = a.cov ? a.cov + os * (int64_t)n * n : nullptr;
     if (m0 < n) {
@@ -410,26 +498,35 @@ __global__ void tail_kernel(Args a)
       return;
     }
     const int ld = m0;
-    PV W = ws, tau = ws + mx * (n + 1), Ri = tau + n;
+    PV<T> W = ws, tau = ws + mx * (n + 1), dv = tau + n, Ri = dv + n;
     for (int q = 0; q < n; ++q)
-      for (int i = 0; i < m0; ++i) W[q * ld + i] = C.G.at(q * mx + i, sb);
-    for (int i = 0; i < m0; ++i) W[n * ld + i] = C.o.at(i, sb);
-    householder(W, ld, m0, n, n + 1, tau);
-    auto Ru = [&](int i, int j) -> double { return W[j * ld + i]; };
-    auto xv = [&](int i) -> double& { return W[n * ld + i]; };
-    bool bad = solve_upper(Ru, n, xv);
-    for (int i = 0; i < n; ++i) x[i] = W[n * ld + i];
+      for (int i = 0; i < m0; ++i) W[q * ld + i] = (T)C.G.at(q * mx + i, sb);
+    for (int i = 0; i < m0; ++i) W[n * ld + i] = (T)C.o.at(i, sb);
+    householder<T>(W, ld, m0, n, n + 1, tau);
+    bool bad = false;
+    for (int i = 0; i < n; ++i) {
+      bad |= (W[i * ld + i] == T(0));
+      dv[i] = T(1) / W[i * ld + i];
+    }
+    if (a.baseR.p)
+      for (int q = 0; q < n; ++q)
+        for (int i = 0; i < n; ++i) a.baseR.at(q * n + i, t) = (i <= q) ? W[q * ld + i] : T(0);
+    auto Ru = [&](int i, int j) -> T { return W[j * ld + i]; };
+    auto Di = [&](int i) -> T { return dv[i]; };
+    auto xv = [&](int i) -> T& { return W[n * ld + i]; };
+    solve_upper(Ru, Di, n, xv);
+    for (int i = 0; i < n; ++i) x[i] = (double)W[n * ld + i];
     if (S) {
       for (int q = 0; q < n; ++q) {
-        for (int i = 0; i < n; ++i) Ri[q * n + i] = (i == q) ? 1.0 : 0.0;
-        auto rc = [&](int i) -> double& { return Ri[q * n + i]; };
-        solve_upper(Ru, n, rc);
+        for (int i = 0; i < n; ++i) Ri[q * n + i] = (i == q) ? T(1) : T(0);
+        auto rc = [&](int i) -> T& { return Ri[q * n + i]; };
+        solve_upper(Ru, Di, n, rc);
       }
       for (int j = 0; j < n; ++j)
         for (int i = 0; i < n; ++i) {
-          double s = 0.0;
+          T s = T(0);
           for (int k = (i > j ? i : j); k < n; ++k) s = fma(Ri[k * n + i], Ri[k * n + j], s);
-          S[(int64_t)j * n + i] = s;
+          S[(int64_t)j * n + i] = (double)s;
         }
     }
     if (bad) atomicOr(a.flag, 2);
@@ -438,33 +535,33 @@ __global__ void tail_kernel(Args a)
 
   /* single last step s = L-1 of an odd-length level (L >= 3) */
   const int64_t s = sb + L - 1;
-  const int64_t es = C.solve[t] + (L - 1) / 2;
-  const int64_t sn = N.slot[t] + L / 2 - 1;
+  const int64_t es = a.ct.solve[t] + (L - 1) / 2;
+  const int64_t sn = a.nt.slot[t] + L / 2 - 1;
   const int ms = C.m[s], mt = ms < n ? ms : n;
   const int ldS = ms > 0 ? ms : 1, ldT = n + mt;
-  PV WS = ws, WT = ws + mx * (n + 1), WF = WT + 2 * n * (2 * n + 1), tau = WF + 2 * n * (n + 1);
+  PV<T> WS = ws, WT = ws + mx * (n + 1), WF = WT + 2 * n * (2 * n + 1), tau = WF + 2 * n * (n + 1);
   /* stage A on [G_s | o_s] */
   for (int q = 0; q < n; ++q)
-    for (int i = 0; i < ms; ++i) WS[q * ldS + i] = C.G.at(q * mx + i, s);
-  for (int i = 0; i < ms; ++i) WS[n * ldS + i] = C.o.at(i, s);
-  householder(WS, ldS, ms, n, n + 1, tau);
+    for (int i = 0; i < ms; ++i) WS[q * ldS + i] = (T)C.G.at(q * mx + i, s);
+  for (int i = 0; i < ms; ++i) WS[n * ldS + i] = (T)C.o.at(i, s);
+  householder<T>(WS, ldS, ms, n, n + 1, tau);
   /* stage B on [H_s F_s c_s; R~_s 0 o'_s] */
   for (int q = 0; q < n; ++q) {
-    for (int i = 0; i < n; ++i) WT[q * ldT + i] = C.H.at(q * n + i, s);
-    for (int i = 0; i < mt; ++i) WT[q * ldT + n + i] = (i <= q) ? WS[q * ldS + i] : 0.0;
-    for (int i = 0; i < n; ++i) WT[(n + q) * ldT + i] = C.F.at(q * n + i, s);
-    for (int i = 0; i < mt; ++i) WT[(n + q) * ldT + n + i] = 0.0;
+    for (int i = 0; i < n; ++i) WT[q * ldT + i] = (T)C.H.at(q * n + i, s);
+    for (int i = 0; i < mt; ++i) WT[q * ldT + n + i] = (i <= q) ? WS[q * ldS + i] : T(0);
+    for (int i = 0; i < n; ++i) WT[(n + q) * ldT + i] = (T)C.F.at(q * n + i, s);
+    for (int i = 0; i < mt; ++i) WT[(n + q) * ldT + n + i] = T(0);
   }
-  for (int i = 0; i < n; ++i) WT[2 * n * ldT + i] = C.c.at(i, s);
+  for (int i = 0; i < n; ++i) WT[2 * n * ldT + i] = (T)C.c.at(i, s);
   for (int i = 0; i < mt; ++i) WT[2 * n * ldT + n + i] = WS[n * ldS + i];
-  householder(WT, ldT, n + mt, n, 2 * n + 1, tau);
+  householder<T>(WT, ldT, n + mt, n, 2 * n + 1, tau);
   for (int q = 0; q < n; ++q)
     for (int i = 0; i < n; ++i) {
-      C.R.at(q * n + i, es) = (i <= q) ? WT[q * ldT + i] : 0.0;
-      C.Ft.at(q * n + i, es) = WT[(n + q) * ldT + i];
-      C.Y.at(q * n + i, es) = 0.0;
+      Rr.R.at(q * n + i, es) = (i <= q) ? WT[q * ldT + i] : T(0);
+      Rr.Ft.at(q * n + i, es) = WT[(n + q) * ldT + i];
+      Rr.Y.at(q * n + i, es) = T(0);
     }
-  for (int i = 0; i < n; ++i) C.cr.at(i, es) = WT[2 * n * ldT + i];
+  for (int i = 0; i < n; ++i) Rr.rhs.at(i, es) = WT[2 * n * ldT + i];
   /* fix-up: QR of [G~_{L-2} o; Z_s o''_s] becomes the next observation */
   const int gp = N.m[sn], rF = gp + mt, ldF = rF > 0 ? rF : 1;
   for (int q = 0; q < n; ++q) {
@@ -473,10 +570,10 @@ __global__ void tail_kernel(Args a)
   }
   for (int i = 0; i < gp; ++i) WF[n * ldF + i] = N.o.at(i, sn);
   for (int i = 0; i < mt; ++i) WF[n * ldF + gp + i] = WT[2 * n * ldT + n + i];
-  householder(WF, ldF, rF, n, n + 1, tau);
+  householder<T>(WF, ldF, rF, n, n + 1, tau);
   const int g2 = rF < n ? rF : n;
   for (int q = 0; q < n; ++q)
-    for (int i = 0; i < g2; ++i) N.G.at(q * mx + i, sn) = (i <= q) ? WF[q * ldF + i] : 0.0;
+    for (int i = 0; i < g2; ++i) N.G.at(q * mx + i, sn) = (i <= q) ? WF[q * ldF + i] : T(0);
   for (int i = 0; i < g2; ++i) N.o.at(i, sn) = WF[n * ldF + i];
   N.m[sn] = g2;
 }
@@ -486,58 +583,71 @@ __global__ void tail_kernel(Args a)
  *
  * With B = [Ft Y] and Sigma = [[Smm Smp]; [Smp^T Spp]] the joint covariance of
  * the odd neighbours (x_{j-1}, x_{j+1}):
- *   x_j            = R^{-1} (cr - Ft x_{j-1} - Y x_{j+1})
+ *   x_j            = R^{-1} (rhs - Ft x_{j-1} - Y x_{j+1})
  *   S_j            = R^{-1} (I + B Sigma B^T) R^{-T}
  *   cov(x_j, x_{j-1}) = -R^{-1} (B Sigma)[:, 0:n]
  *   cov(x_j, x_{j+1}) = -R^{-1} (B Sigma)[:, n:2n]
  * (the reference's formulas, Solve_Estimates 703-903, grouped by columns of
- * B Sigma, which are streamed one at a time).
+ * B Sigma, which are streamed one at a time).  In a refinement sweep the
+ * right-hand side is y (yrhs) and `state` holds the correction d.
  * ------------------------------------------------------------------------ */
-__global__ void solve_kernel(Args a, int want_cov)
+template <typename T, int NT = 0, int BS = 0>
+__global__ void __launch_bounds__(BS ? BS : 1024) solve_kernel(Args<T, T> a, int want_cov)
 {
-  extern __shared__ double smem[];
+  extern __shared__ unsigned char smem_raw[];
+  T* smem = reinterpret_cast<T*>(smem_raw);
   const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (item >= a.cur.nsolve) return;
-  const int n = a.n;
+  if (item >= a.ct.nsolve) return;
+  const int n = NT ? NT : a.n;
   const int64_t nn = (int64_t)n * n;
-  const LevelDev& C = a.cur;
-  const LevelDev& N = a.nxt;
-  const int t = find_track(C.solve, a.ntracks, item);
-  const int64_t e = item - C.solve[t];
-  const int64_t j = 2 * e, L = C.L[t];
+  const Rec<T>& Rr = a.cr;
+  const int t = find_track(a.ct.solve, a.ntracks, item);
+  const int64_t e = item - a.ct.solve[t];
+  const int64_t j = 2 * e, L = a.ct.L[t];
   const bool hp = j > 0, hn = j + 1 < L;
   const int64_t se = item; /* records are indexed by the solve prefix */
-  const int64_t oj = orig_step(a, t, j), om = hp ? orig_step(a, t, j - 1) : 0, op = hn ? orig_step(a, t, j + 1) : 0;
+  const int64_t oj = orig_step(a.track_start, a.level, t, j);
+  const int64_t om = hp ? orig_step(a.track_start, a.level, t, j - 1) : 0;
+  const int64_t op = hn ? orig_step(a.track_start, a.level, t, j + 1) : 0;
 
-  PV ws{smem + threadIdx.x, (int)blockDim.x};
-  PV Rs = ws, Fs = ws + n * n, Ys = ws + 2 * n * n, M = ws + 3 * n * n, sg = ws + 4 * n * n, pv = sg + 2 * n;
+  using View = typename ViewOf<T, BS>::type;
+  View ws = ViewOf<T, BS>::make(smem);
+  View Rs = ws, Fs = ws + n * n, Ys = ws + 2 * n * n, M = ws + 3 * n * n, sg = ws + 4 * n * n, pv = sg + 2 * n,
+       dv = pv + n;
+  bool bad = false;
   for (int k = 0; k < n * n; ++k) {
-    Rs[k] = C.R.at(k, se);
-    Fs[k] = hp ? C.Ft.at(k, se) : 0.0;
-    Ys[k] = hn ? C.Y.at(k, se) : 0.0;
+    Rs[k] = Rr.R.at(k, se);
+    Fs[k] = hp ? Rr.Ft.at(k, se) : T(0);
+    Ys[k] = hn ? Rr.Y.at(k, se) : T(0);
   }
-  auto Ru = [&](int i, int jj) -> double { return Rs[jj * n + i]; };
+  for (int i = 0; i < n; ++i) {
+    const T d = Rs[i * n + i];
+    bad |= (d == T(0));
+    dv[i] = T(1) / d;
+  }
+  auto Ru = [&](int i, int jj) -> T { return Rs[jj * n + i]; };
+  auto Di = [&](int i) -> T { return dv[i]; };
 
   /* state */
-  for (int i = 0; i < n; ++i) pv[i] = C.cr.at(i, se);
+  for (int i = 0; i < n; ++i) pv[i] = a.yrhs.p ? a.yrhs.at(i, se) : Rr.rhs.at(i, se);
   if (hp) {
     const double* xm = a.state + om * n;
     for (int k = 0; k < n; ++k) {
-      const double xk = xm[k];
+      const T xk = (T)xm[k];
       for (int i = 0; i < n; ++i) pv[i] = fma(-Fs[k * n + i], xk, pv[i]);
     }
   }
   if (hn) {
     const double* xp = a.state + op * n;
     for (int k = 0; k < n; ++k) {
-      const double xk = xp[k];
+      const T xk = (T)xp[k];
       for (int i = 0; i < n; ++i) pv[i] = fma(-Ys[k * n + i], xk, pv[i]);
     }
   }
-  auto pvr = [&](int i) -> double& { return pv[i]; };
-  bool bad = solve_upper(Ru, n, pvr);
+  auto pvr = [&](int i) -> T& { return pv[i]; };
+  solve_upper(Ru, Di, n, pvr);
   double* xo = a.state + oj * n;
-  for (int i = 0; i < n; ++i) xo[i] = pv[i];
+  for (int i = 0; i < n; ++i) xo[i] = (double)pv[i];
   if (!want_cov) {
     if (bad) atomicOr(a.flag, 2);
     return;
@@ -545,68 +655,248 @@ __global__ void solve_kernel(Args a, int want_cov)
 
   const double* Smm = hp ? a.cov + om * nn : nullptr;
   const double* Spp = hn ? a.cov + op * nn : nullptr;
-  const int64_t smp = (hp && hn) ? N.slot[t] + (j + 1) / 2 : 0; /* U of the next level */
-  for (int k = 0; k < n * n; ++k) M[k] = 0.0;
+  const int64_t smp = (hp && hn) ? a.nt.slot[t] + (j + 1) / 2 : 0; /* U of the next level */
+  for (int k = 0; k < n * n; ++k) M[k] = T(0);
   const int q0 = hp ? 0 : n, q1 = hn ? 2 * n : n;
   for (int q = q0; q < q1; ++q) {
     /* column q of Sigma */
     if (q < n) {
-      for (int i = 0; i < n; ++i) sg[i] = Smm[(int64_t)q * n + i];
-      for (int i = 0; i < n; ++i) sg[n + i] = hn ? N.U.at(i * n + q, smp) : 0.0; /* Smp^T[:, q] = Smp[q, :] */
+      for (int i = 0; i < n; ++i) sg[i] = (T)Smm[(int64_t)q * n + i];
+      for (int i = 0; i < n; ++i) sg[n + i] = hn ? a.nr.U.at(i * n + q, smp) : T(0); /* Smp[q, :] */
     } else {
       const int qq = q - n;
-      for (int i = 0; i < n; ++i) sg[i] = hp ? N.U.at(qq * n + i, smp) : 0.0;
-      for (int i = 0; i < n; ++i) sg[n + i] = Spp[(int64_t)qq * n + i];
+      for (int i = 0; i < n; ++i) sg[i] = hp ? a.nr.U.at(qq * n + i, smp) : T(0);
+      for (int i = 0; i < n; ++i) sg[n + i] = (T)Spp[(int64_t)qq * n + i];
     }
     /* pv = B sigma */
-    for (int i = 0; i < n; ++i) pv[i] = 0.0;
+    for (int i = 0; i < n; ++i) pv[i] = T(0);
     if (hp)
       for (int k = 0; k < n; ++k) {
-        const double sk = sg[k];
+        const T sk = sg[k];
         for (int i = 0; i < n; ++i) pv[i] = fma(Fs[k * n + i], sk, pv[i]);
       }
     if (hn)
       for (int k = 0; k < n; ++k) {
-        const double sk = sg[n + k];
+        const T sk = sg[n + k];
         for (int i = 0; i < n; ++i) pv[i] = fma(Ys[k * n + i], sk, pv[i]);
       }
     /* M += pv b_q^T, b_q = column q of B */
-    PV bq = q < n ? Fs + q * n : Ys + (q - n) * n;
+    View bq = q < n ? Fs + q * n : Ys + (q - n) * n;
     for (int c = 0; c < n; ++c) {
-      const double bc = bq[c];
+      const T bc = bq[c];
       for (int i = 0; i < n; ++i) M[c * n + i] = fma(pv[i], bc, M[c * n + i]);
     }
-    /* off-diagonal block column: -R^{-1} pv */
-    solve_upper(Ru, n, pvr);
     if (a.level == 0) continue; /* level 0's off-diagonal blocks are not needed */
+    /* off-diagonal block column: -R^{-1} pv */
+    solve_upper(Ru, Di, n, pvr);
     if (q < n) { /* cov(x_{j-1}, x_j) = cov(x_j, x_{j-1})^T: row q */
-      const int64_t sU = C.slot[t] + j;
-      for (int i = 0; i < n; ++i) C.U.at(i * n + q, sU) = -pv[i];
+      const int64_t sU = a.ct.slot[t] + j;
+      for (int i = 0; i < n; ++i) Rr.U.at(i * n + q, sU) = -pv[i];
     } else {
-      const int64_t sU = C.slot[t] + j + 1;
-      for (int i = 0; i < n; ++i) C.U.at((q - n) * n + i, sU) = -pv[i];
+      const int64_t sU = a.ct.slot[t] + j + 1;
+      for (int i = 0; i < n; ++i) Rr.U.at((q - n) * n + i, sU) = -pv[i];
     }
   }
-  for (int i = 0; i < n; ++i) M[i * n + i] += 1.0;
+  for (int i = 0; i < n; ++i) M[i * n + i] += T(1);
   /* S = R^{-1} M R^{-T}: solve the columns, transpose, solve again, transpose */
   for (int c = 0; c < n; ++c) {
-    auto mc = [&](int i) -> double& { return M[c * n + i]; };
-    solve_upper(Ru, n, mc);
+    auto mc = [&](int i) -> T& { return M[c * n + i]; };
+    solve_upper(Ru, Di, n, mc);
   }
   for (int c = 0; c < n; ++c)
     for (int i = c + 1; i < n; ++i) {
-      const double tmp = M[c * n + i];
+      const T tmp = M[c * n + i];
       M[c * n + i] = M[i * n + c];
       M[i * n + c] = tmp;
     }
   for (int c = 0; c < n; ++c) {
-    auto mc = [&](int i) -> double& { return M[c * n + i]; };
-    solve_upper(Ru, n, mc);
+    auto mc = [&](int i) -> T& { return M[c * n + i]; };
+    solve_upper(Ru, Di, n, mc);
   }
   double* So = a.cov + oj * nn;
   for (int c = 0; c < n; ++c)
-    for (int i = 0; i < n; ++i) So[(int64_t)c * n + i] = M[i * n + c];
+    for (int i = 0; i < n; ++i) So[(int64_t)c * n + i] = (double)M[i * n + c];
   if (bad) atomicOr(a.flag, 2);
+}
+
+/* ---------------------------------------------------------------------------
+ * refinement sweep kernels (FP32 factors, FP64 residual)
+ * ------------------------------------------------------------------------ */
+
+/* w <- Cov^{-1} w for a covariance factor (cov, type): with Cov^{-1} = V^T V
+ * for the weighing V of kalman_covariance_matrix_weigh -- 'W': W^T (W w),
+ * 'w': diag(cov)^2 w, 'C': L^{-T} L^{-1} w (L = chol(cov)), 'U'/'F':
+ * L^{-T} L^{-1} w (L = tril(cov)).  FP64; L, dinv, tmp as in weigh_column.  */
+__device__ bool apply_precision(char type, const double* cov, int ldc, int rows, PV<double> L, PV<double> dinv,
+                                PV<double> w, PV<double> tmp)
+{
+  if (type == 'W') {
+    for (int i = 0; i < rows; ++i) {
+      double s = 0.0;
+      for (int j = 0; j < rows; ++j) s = fma(cov[(int64_t)j * ldc + i], w[j], s);
+      tmp[i] = s;
+    }
+    for (int j = 0; j < rows; ++j) {
+      double s = 0.0;
+      for (int i = 0; i < rows; ++i) s = fma(cov[(int64_t)j * ldc + i], tmp[i], s);
+      w[j] = s;
+    }
+    return true;
+  }
+  if (type == 'w') {
+    for (int i = 0; i < rows; ++i) w[i] *= cov[i] * cov[i];
+    return true;
+  }
+  const bool ok = lower_factor(type, cov, ldc, rows, L, dinv);
+  for (int j = 0; j < rows; ++j) { /* L^{-1} */
+    const double xj = w[j] * dinv[j];
+    w[j] = xj;
+    for (int i = j + 1; i < rows; ++i) w[i] = fma(-xj, L[j * rows + i], w[i]);
+  }
+  for (int j = rows - 1; j >= 0; --j) { /* L^{-T} */
+    double s = w[j];
+    for (int i = j + 1; i < rows; ++i) s = fma(-L[j * rows + i], w[i], s);
+    w[j] = s * dinv[j];
+  }
+  return ok;
+}
+
+/* The refinement's right-hand side z = A^T (b - A x) of the weighted
+ * least-squares system, in FP64 from the caller's raw equations.  With the
+ * raw residuals r_i = c_i + F_i x_{i-1} - H_i x_i and s_i = o_i - G_i x_i:
+ *   wE_i = K_i^{-1} r_i,   z_i = H_i^T wE_i + G_i^T C_i^{-1} s_i - F_{i+1}^T wE_{i+1}.
+ * residual_kernel stores wE_i and the first two terms; atr_kernel adds the
+ * third and rounds z to FP32.  FP64 is needed: at the solution r is the
+ * (nonzero) least-squares residual, and z -> 0 is formed by cancellation.    */
+__global__ void residual_kernel(Args<float, float> a, RawDev raw, Soa<double> wE, Soa<double> zp, int64_t nsteps)
+{
+  extern __shared__ unsigned char smem_raw[];
+  double* smem = reinterpret_cast<double*>(smem_raw);
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nsteps) return;
+  const int n = a.n, mx = a.mx, mm = raw.mmax;
+  PV<double> ws{smem + threadIdx.x, (int)blockDim.x};
+  PV<double> L = ws, dinv = ws + mx * mx, w = dinv + mx, tmp = w + mx, z = tmp + mx;
+  const int t = find_track(a.track_start, a.ntracks, g);
+  const int64_t i = g - a.track_start[t];
+  const int64_t q = a.ct.slot[t] + i;
+  const int64_t nn = (int64_t)n * n;
+  const double* x = a.state + g * n;
+  for (int c = 0; c < n; ++c) z[c] = 0.0;
+  if (i > 0) {
+    const double* xm = x - n;
+    const double* H = raw.H + g * nn;
+    const double* F = raw.F + g * nn;
+    for (int p = 0; p < n; ++p) {
+      double s = raw.c[g * n + p];
+      for (int c = 0; c < n; ++c) s = fma(F[c * n + p], xm[c], fma(-H[c * n + p], x[c], s));
+      w[p] = s;
+    }
+    apply_precision(raw.K_type[g], raw.K + g * nn, n, n, L, dinv, w, tmp);
+    for (int p = 0; p < n; ++p) wE.at(p, q) = w[p];
+    for (int c = 0; c < n; ++c) {
+      double s = z[c];
+      for (int p = 0; p < n; ++p) s = fma(H[c * n + p], w[p], s);
+      z[c] = s;
+    }
+  }
+  const int m = a.ce.m[q];
+  if (m > 0) {
+    const double* G = raw.G + g * (int64_t)mm * n;
+    for (int p = 0; p < m; ++p) {
+      double s = raw.o[g * mm + p];
+      for (int c = 0; c < n; ++c) s = fma(-G[(int64_t)c * mm + p], x[c], s);
+      w[p] = s;
+    }
+    apply_precision(raw.C_type[g], raw.C + g * (int64_t)mm * mm, mm, m, L, dinv, w, tmp);
+    for (int c = 0; c < n; ++c) {
+      double s = z[c];
+      for (int p = 0; p < m; ++p) s = fma(G[(int64_t)c * mm + p], w[p], s);
+      z[c] = s;
+    }
+  }
+  for (int c = 0; c < n; ++c) zp.at(c, q) = z[c];
+}
+
+__global__ void atr_kernel(Args<float, float> a, RawDev raw, Soa<double> wE, Soa<double> zp, Soa<float> z0,
+                           int64_t nsteps)
+{
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nsteps) return;
+  const int n = a.n;
+  const int t = find_track(a.track_start, a.ntracks, g);
+  const int64_t g0 = a.track_start[t], k = a.track_start[t + 1] - g0, i = g - g0;
+  const int64_t q = a.ct.slot[t] + i;
+  const double* F1 = raw.F + (g + 1) * (int64_t)n * n;
+  for (int c = 0; c < n; ++c) {
+    double s = zp.at(c, q);
+    if (i + 1 < k)
+      for (int p = 0; p < n; ++p) s = fma(-F1[c * n + p], wE.at(p, q + 1), s);
+    z0.at(c, q) = (float)s;
+  }
+}
+
+/* R^T y = z, even steps of a level: y_j = R_j^{-T} z_j                       */
+__global__ void rt_even_kernel(Args<float, float> a, Soa<float> zc, Soa<float> yc)
+{
+  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= a.ct.nsolve) return;
+  const int n = a.n;
+  const int t = find_track(a.ct.solve, a.ntracks, item);
+  const int64_t j = 2 * (item - a.ct.solve[t]);
+  const int64_t sz = a.ct.slot[t] + j;
+  const Soa<float>& R = a.cr.R;
+  auto Ru = [&](int i, int jj) -> float { return R.at(jj * n + i, item); };
+  auto Di = [&](int i) -> float { return 1.0f / R.at(i * n + i, item); };
+  auto yv = [&](int i) -> float& { return yc.at(i, item); };
+  for (int i = 0; i < n; ++i) yc.at(i, item) = zc.at(i, sz);
+  solve_upper_t(Ru, Di, n, yv);
+}
+
+/* the odd steps' right-hand sides lose the even rows' contributions and
+ * become the next level's: z' = z_{2p+1} - Y_{2p}^T y_{2p} - Ft_{2p+2}^T y_{2p+2} */
+__global__ void rt_odd_kernel(Args<float, float> a, Soa<float> zc, Soa<float> yc, Soa<float> zn)
+{
+  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= a.ct.npairs) return;
+  const int n = a.n;
+  const int t = find_track(a.ct.pair, a.ntracks, item);
+  const int64_t p = item - a.ct.pair[t], L = a.ct.L[t];
+  const int64_t so = a.ct.slot[t] + 2 * p + 1, sn = a.nt.slot[t] + p;
+  const int64_t e0 = a.ct.solve[t] + p, e1 = e0 + 1;
+  const bool right = 2 * p + 2 <= L - 1;
+  for (int c = 0; c < n; ++c) {
+    float s = zc.at(c, so);
+    for (int r = 0; r < n; ++r) s = fma(-a.cr.Y.at(c * n + r, e0), yc.at(r, e0), s);
+    if (right)
+      for (int r = 0; r < n; ++r) s = fma(-a.cr.Ft.at(c * n + r, e1), yc.at(r, e1), s);
+    zn.at(c, sn) = s;
+  }
+}
+
+/* one-step levels: d = R_b^{-1} R_b^{-T} z                                   */
+__global__ void rt_base_kernel(Args<float, float> a, Soa<float> zc, Soa<float> tmp)
+{
+  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= a.ct.ntail) return;
+  const int n = a.n;
+  const int t = (int)a.ct.tail[item];
+  if (a.ct.L[t] != 1) return;
+  const int64_t sz = a.ct.slot[t];
+  auto Ru = [&](int i, int jj) -> float { return a.baseR.at(jj * n + i, t); };
+  auto Di = [&](int i) -> float { return 1.0f / a.baseR.at(i * n + i, t); };
+  auto v = [&](int i) -> float& { return tmp.at(i, item); };
+  for (int i = 0; i < n; ++i) tmp.at(i, item) = zc.at(i, sz);
+  solve_upper_t(Ru, Di, n, v);
+  solve_upper(Ru, Di, n, v);
+  double* d = a.state + orig_step(a.track_start, a.level, t, 0) * n;
+  for (int i = 0; i < n; ++i) d[i] = (double)tmp.at(i, item);
+}
+
+__global__ void add_kernel(double* x, const double* d, int64_t count)
+{
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < count) x[g] += d[g];
 }
 
 /* ---------------------------------------------------------------------------
@@ -623,11 +913,17 @@ struct LevelPlan {
  * (host copy, uploaded into the workspace) and the workspace layout.        */
 struct Plan {
   int nlev = 0;
+  bool fp32 = false, refine = false;
   LevelPlan lp[kMaxLevels];
   size_t tab_entries = 0, off_ts = 0;
-  size_t o_tab = 0, o_flag = 0, o_eq[2] = {0, 0}, o_m[2] = {0, 0}, o_rec[kMaxLevels] = {0}, o_U[kMaxLevels] = {0};
+  size_t o_tab = 0, o_flag = 0;
+  size_t o_eq0 = 0, o_m0 = 0;      /* level 0 (T)                            */
+  size_t o_eqA = 0, o_mA = 0;      /* odd levels (T)                         */
+  size_t o_eqB = 0, o_mB = 0;      /* even levels >= 2 in FP32 mode          */
+  size_t o_rec[kMaxLevels] = {0}, o_U[kMaxLevels] = {0};
+  size_t o_z[kMaxLevels] = {0}, o_y[kMaxLevels] = {0}, o_baseR = 0, o_dx = 0, o_tmp = 0, o_rE = 0, o_rO = 0;
   size_t bytes = 0;
-  int64_t S0 = 0, S1 = 0;
+  int64_t S0 = 0, S1 = 0, S2 = 0;
 };
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -635,11 +931,14 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 /* Builds the plan.  Track t has k_t >> l steps at level l.  When tab is not
  * NULL the tables are written into it (tab_cap entries).  Returns the number
  * of table entries needed, or 0 if the recursion is deeper than kMaxLevels. */
-size_t build_plan(const kalman_gpu_problem_t* p, bool want_cov, Plan& P, int64_t* tab, size_t tab_cap)
+size_t build_plan(const kalman_gpu_problem_t* p, bool want_cov, bool fp32, bool refine, Plan& P, int64_t* tab,
+                  size_t tab_cap)
 {
   const int n = p->n, T = p->ntracks;
   const int mx = p->mmax > n ? p->mmax : n;
   const int64_t nn = (int64_t)n * n;
+  P.fp32 = fp32;
+  P.refine = refine;
   int64_t kmax = 0;
   for (int t = 0; t < T; ++t) kmax = std::max<int64_t>(kmax, p->track_start[t + 1] - p->track_start[t]);
   P.nlev = 1;
@@ -678,22 +977,39 @@ size_t build_plan(const kalman_gpu_problem_t* p, bool want_cov, Plan& P, int64_t
   for (int t = 0; t <= T; ++t) put(p->track_start[t]);
   P.tab_entries = pos;
 
-  /* workspace layout; level equations ping-pong between two regions sized
-     for levels 0 and 1, records and off-diagonal blocks per level           */
+  /* workspace layout */
+  const size_t ts = fp32 ? sizeof(float) : sizeof(double);
   size_t bytes = 0;
   auto take = [&](size_t b) { size_t o = bytes; bytes = align_up(bytes + b, 256); return o; };
   P.o_tab = take(pos * sizeof(int64_t));
   P.o_flag = take(sizeof(int));
-  const int64_t eq_doubles_per_slot = 2 * nn + n + (int64_t)mx * n + mx;
-  P.S0 = P.lp[0].S;
-  P.S1 = P.nlev > 1 ? P.lp[1].S : 0;
-  P.o_eq[0] = take((size_t)std::max<int64_t>(P.S0, 1) * eq_doubles_per_slot * sizeof(double));
-  P.o_m[0] = take((size_t)std::max<int64_t>(P.S0, 1) * sizeof(int32_t));
-  P.o_eq[1] = take((size_t)std::max<int64_t>(P.S1, 1) * eq_doubles_per_slot * sizeof(double));
-  P.o_m[1] = take((size_t)std::max<int64_t>(P.S1, 1) * sizeof(int32_t));
+  const int64_t eqd = 2 * nn + n + (int64_t)mx * n + mx; /* equation entries per slot */
+  P.S0 = std::max<int64_t>(P.lp[0].S, 1);
+  P.S1 = std::max<int64_t>(P.nlev > 1 ? P.lp[1].S : 0, 1);
+  P.S2 = std::max<int64_t>(P.nlev > 2 ? P.lp[2].S : 0, 1);
+  P.o_eq0 = take((size_t)P.S0 * eqd * ts);
+  P.o_m0 = take((size_t)P.S0 * sizeof(int32_t));
+  P.o_eqA = take((size_t)P.S1 * eqd * ts);
+  P.o_mA = take((size_t)P.S1 * sizeof(int32_t));
+  if (fp32) {
+    P.o_eqB = take((size_t)P.S2 * eqd * ts);
+    P.o_mB = take((size_t)P.S2 * sizeof(int32_t));
+  }
   for (int l = 0; l < P.nlev; ++l) {
-    P.o_rec[l] = take((size_t)std::max<int64_t>(P.lp[l].E, 1) * (3 * nn + n) * sizeof(double));
-    P.o_U[l] = (want_cov && l > 0) ? take((size_t)std::max<int64_t>(P.lp[l].S, 1) * nn * sizeof(double)) : 0;
+    const int64_t E = std::max<int64_t>(P.lp[l].E, 1), S = std::max<int64_t>(P.lp[l].S, 1);
+    P.o_rec[l] = take((size_t)E * (3 * nn + n) * ts);
+    P.o_U[l] = (want_cov && l > 0) ? take((size_t)S * nn * ts) : 0;
+    if (refine) {
+      P.o_z[l] = take((size_t)S * n * sizeof(float));
+      P.o_y[l] = take((size_t)E * n * sizeof(float));
+    }
+  }
+  if (refine) {
+    P.o_baseR = take((size_t)std::max(T, 1) * nn * sizeof(float));
+    P.o_tmp = take((size_t)std::max(T, 1) * n * sizeof(float));
+    P.o_dx = take((size_t)std::max<int64_t>(p->nsteps, 1) * n * sizeof(double));
+    P.o_rE = take((size_t)P.S0 * n * sizeof(double));
+    P.o_rO = take((size_t)P.S0 * n * sizeof(double));
   }
   P.bytes = bytes;
   return pos;
@@ -715,12 +1031,64 @@ int pick_block(size_t per_thread_bytes, int preferred, int* block)
   return 0;
 }
 
+template <typename T>
+Eq<T> eq_at(char* B, size_t off, size_t off_m, int64_t stride, int n, int mx)
+{
+  const int64_t nn = (int64_t)n * n;
+  T* e = (T*)(B + off);
+  Eq<T> d;
+  d.F = Soa<T>{e, stride};
+  d.H = Soa<T>{e + nn * stride, stride};
+  d.c = Soa<T>{e + 2 * nn * stride, stride};
+  d.G = Soa<T>{e + (2 * nn + n) * stride, stride};
+  d.o = Soa<T>{e + (2 * nn + n + (int64_t)mx * n) * stride, stride};
+  d.m = (int32_t*)(B + off_m);
+  return d;
+}
+
+/* The pair and solve kernels used for a state dimension: instantiations with
+ * compile-time n, mx and block size for the common small shapes, the
+ * runtime-dimension kernels otherwise.                                       */
+template <typename T>
+struct Kernels {
+  void (*pair)(Args<T, T>, int) = nullptr;
+  void (*solve)(Args<T, T>, int) = nullptr;
+  int bp = 0, bs = 0; /* fixed block sizes of the specialised kernels (0: pick) */
+};
+
+template <typename T>
+Kernels<T> choose_kernels(int n, int mx)
+{
+  Kernels<T> k;
+  if (n == mx && n == 6) {
+    k.pair = pair_kernel<T, T, 6, 6, 128>;
+    k.solve = solve_kernel<T, 6, 64>;
+    k.bp = 128;
+    k.bs = 64;
+  } else if (n == mx && n == 4) {
+    k.pair = pair_kernel<T, T, 4, 4, 128>;
+    k.solve = solve_kernel<T, 4, 64>;
+    k.bp = 128;
+    k.bs = 64;
+  } else if (n == mx && n == 8) {
+    k.pair = pair_kernel<T, T, 8, 8, 128>;
+    k.solve = solve_kernel<T, 8, 64>;
+    k.bp = 128;
+    k.bs = 64;
+  } else {
+    k.pair = pair_kernel<T, T>;
+    k.solve = solve_kernel<T>;
+  }
+  return k;
+}
+
 /* Uploads the tables, runs every kernel of the smoother on stream st using
  * the device workspace at B (at least P.bytes), waits, reports the flags.   */
+template <typename T>
 int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, const Plan& P, const int64_t* tab,
              char* B)
 {
-  const int n = p->n, T = p->ntracks, nlev = P.nlev;
+  const int n = p->n, T_ = p->ntracks, nlev = P.nlev;
   const int mx = p->mmax > n ? p->mmax : n;
   const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
   const int64_t nn = (int64_t)n * n;
@@ -730,26 +1098,11 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
   cudaMemcpyAsync(dtab, tab, P.tab_entries * sizeof(int64_t), cudaMemcpyHostToDevice, st);
   cudaMemsetAsync(dflag, 0, sizeof(int), st);
 
-  auto level_dev = [&](int l) {
-    LevelDev d;
+  auto tables = [&](int l) {
+    Tables d;
     memset(&d, 0, sizeof(d));
     if (l >= nlev) return d;
     const LevelPlan& L = lp[l];
-    const int64_t Sr = (l & 1) ? std::max<int64_t>(P.S1, 1) : std::max<int64_t>(P.S0, 1); /* region stride */
-    double* eq = (double*)(B + P.o_eq[l & 1]);
-    d.F = Soa{eq, Sr};
-    d.H = Soa{eq + nn * Sr, Sr};
-    d.c = Soa{eq + 2 * nn * Sr, Sr};
-    d.G = Soa{eq + (2 * nn + n) * Sr, Sr};
-    d.o = Soa{eq + (2 * nn + n + (int64_t)mx * n) * Sr, Sr};
-    d.m = (int32_t*)(B + P.o_m[l & 1]);
-    const int64_t E = std::max<int64_t>(L.E, 1);
-    double* rec = (double*)(B + P.o_rec[l]);
-    d.R = Soa{rec, E};
-    d.Ft = Soa{rec + nn * E, E};
-    d.Y = Soa{rec + 2 * nn * E, E};
-    d.cr = Soa{rec + 3 * nn * E, E};
-    d.U = (want_cov && l > 0) ? Soa{(double*)(B + P.o_U[l]), std::max<int64_t>(L.S, 1)} : Soa{nullptr, 0};
     d.L = dtab + L.off_L;
     d.slot = dtab + L.off_slot;
     d.pair = dtab + L.off_pair;
@@ -760,59 +1113,153 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
     d.ntail = L.ntail;
     return d;
   };
-
-  Args a;
-  memset(&a, 0, sizeof(a));
-  a.n = n;
-  a.mx = mx;
-  a.ntracks = T;
-  a.track_start = dtab + P.off_ts;
-  a.state = p->state;
-  a.cov = want_cov ? p->covariance : nullptr;
-  a.flag = dflag;
+  auto eq0 = [&]() { return eq_at<T>(B, P.o_eq0, P.o_m0, P.S0, n, mx); };
+  auto eqT = [&](int l) { /* equations of level l >= 1 in the arithmetic type */
+    if (l & 1) return eq_at<T>(B, P.o_eqA, P.o_mA, P.S1, n, mx);
+    if (P.fp32) return eq_at<T>(B, P.o_eqB, P.o_mB, P.S2, n, mx);
+    return eq_at<T>(B, P.o_eq0, P.o_m0, P.S0, n, mx); /* FP64: even levels reuse level 0's region */
+  };
+  auto rec = [&](int l) {
+    Rec<T> r;
+    memset(&r, 0, sizeof(r));
+    if (l >= nlev) return r;
+    const int64_t E = std::max<int64_t>(lp[l].E, 1);
+    T* d = (T*)(B + P.o_rec[l]);
+    r.R = Soa<T>{d, E};
+    r.Ft = Soa<T>{d + nn * E, E};
+    r.Y = Soa<T>{d + 2 * nn * E, E};
+    r.rhs = Soa<T>{d + 3 * nn * E, E};
+    if (want_cov && l > 0) r.U = Soa<T>{(T*)(B + P.o_U[l]), std::max<int64_t>(lp[l].S, 1)};
+    return r;
+  };
 
   /* ---- launch configuration ---- */
   const int rmax = 2 * mx;
-  const size_t pt_weigh = (size_t)(mx * mx + 2 * mx) * sizeof(double);
-  const size_t pt_pair = (size_t)(rmax * (n + 1) + n + rmax) * sizeof(double);
-  const size_t pt_tail = (size_t)(mx * (n + 1) + 2 * n * (2 * n + 1) + 2 * n * (n + 1) + n + nn) * sizeof(double);
-  const size_t pt_solve = (size_t)(4 * nn + 3 * n) * sizeof(double);
-  int bw, bp, bt, bs;
+  const size_t ts = sizeof(T);
+  const size_t pt_weigh = (size_t)(mx * mx + 3 * mx) * ts;
+  const size_t pt_pair = (size_t)(rmax * (n + 1) + n + rmax) * ts;
+  const size_t pt_tail = (size_t)(mx * (n + 1) + 2 * n * (2 * n + 1) + 2 * n * (n + 1) + 2 * n + nn) * ts;
+  const size_t pt_solve = (size_t)(4 * nn + 4 * n) * ts;
+  const size_t pt_res = (size_t)(mx * mx + 3 * mx + n) * sizeof(double);
+  int bw, bp, bt, bs, br;
   if (pick_block(pt_weigh, 128, &bw) || pick_block(pt_pair, 128, &bp) || pick_block(pt_tail, 32, &bt) ||
-      pick_block(pt_solve, 64, &bs))
+      pick_block(pt_solve, 64, &bs) || pick_block(pt_res, 128, &br))
     return ukg_set_error(KALMAN_GPU_EINVAL, "state dimension %d (observation rows %d) needs more shared memory per "
                          "thread than this build's odd-even kernels use", n, mx);
-  cudaFuncSetAttribute(weigh_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bw * pt_weigh));
-  cudaFuncSetAttribute(pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bp * pt_pair));
-  cudaFuncSetAttribute(tail_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bt * pt_tail));
-  cudaFuncSetAttribute(solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bs * pt_solve));
+  const Kernels<T> K = choose_kernels<T>(n, mx);
+  if (K.bp) bp = K.bp;
+  if (K.bs) bs = K.bs;
+  cudaFuncSetAttribute(weigh_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bw * pt_weigh));
+  cudaFuncSetAttribute(K.pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bp * pt_pair));
+  cudaFuncSetAttribute(tail_kernel<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bt * pt_tail));
+  cudaFuncSetAttribute(K.solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bs * pt_solve));
+  cudaFuncSetAttribute(residual_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(br * pt_res));
 
   auto grid = [](int64_t items, int block) { return (unsigned)((items + block - 1) / block); };
+  const int kPair = P.fp32 ? UKG_K_PAIR32 : UKG_K_PAIR;
+  const int kSolve = P.fp32 ? UKG_K_SOLVE32 : UKG_K_SOLVE;
+  Soa<T> baseR{P.refine ? (T*)(B + P.o_baseR) : nullptr, std::max(T_, 1)};
 
   /* ---- level 0: weighing ---- */
+  const RawDev raw{p->H, p->F, p->c, p->K, p->G, p->o, p->C, p->K_type, p->C_type, p->obs_rows, p->mmax};
   {
-    a.level = 0;
-    a.cur = level_dev(0);
-    RawDev raw{p->H, p->F, p->c, p->K, p->G, p->o, p->C, p->K_type, p->C_type, p->obs_rows, p->mmax};
-    UKG_LAUNCH(UKG_K_WEIGH, st, (weigh_kernel<<<grid(p->nsteps, bw), bw, bw * pt_weigh, st>>>(a, raw, p->nsteps)));
+    Args<T, T> w;
+    memset(&w, 0, sizeof(w));
+    w.ct = tables(0);
+    w.ce = eq0();
+    w.n = n;
+    w.mx = mx;
+    w.ntracks = T_;
+    w.track_start = dtab + P.off_ts;
+    w.flag = dflag;
+    UKG_LAUNCH(UKG_K_WEIGH, st,
+               (weigh_kernel<T><<<grid(p->nsteps, bw), bw, bw * pt_weigh, st>>>(w, raw, p->nsteps)));
   }
+  auto common = [&](auto& a, int l) {
+    a.ct = tables(l);
+    a.nt = tables(l + 1);
+    a.cr = rec(l);
+    a.nr = rec(l + 1);
+    a.n = n;
+    a.mx = mx;
+    a.level = l;
+    a.ntracks = T_;
+    a.track_start = dtab + P.off_ts;
+    a.state = p->state;
+    a.cov = want_cov ? p->covariance : nullptr;
+    a.flag = dflag;
+    a.baseR = baseR;
+  };
   /* ---- forward elimination ---- */
   for (int l = 0; l < nlev; ++l) {
-    a.level = l;
-    a.cur = level_dev(l);
-    a.nxt = level_dev(l + 1);
+    Args<T, T> a;
+    memset(&a, 0, sizeof(a));
+    common(a, l);
+    a.ce = l == 0 ? eq0() : eqT(l);
+    if (l + 1 < nlev) a.ne = eqT(l + 1);
     if (lp[l].npairs > 0)
-      UKG_LAUNCH(UKG_K_PAIR, st, (pair_kernel<<<grid(lp[l].npairs, bp), bp, bp * pt_pair, st>>>(a, rmax)));
-    if (lp[l].ntail > 0) UKG_LAUNCH(UKG_K_TAIL, st, (tail_kernel<<<grid(lp[l].ntail, bt), bt, bt * pt_tail, st>>>(a)));
+      UKG_LAUNCH(kPair, st, (K.pair<<<grid(lp[l].npairs, bp), bp, bp * pt_pair, st>>>(a, rmax)));
+    if (lp[l].ntail > 0)
+      UKG_LAUNCH(UKG_K_TAIL, st, (tail_kernel<T, T><<<grid(lp[l].ntail, bt), bt, bt * pt_tail, st>>>(a)));
   }
   /* ---- back-substitution ---- */
   for (int l = nlev - 2; l >= 0; --l) {
-    a.level = l;
-    a.cur = level_dev(l);
-    a.nxt = level_dev(l + 1);
+    Args<T, T> a;
+    memset(&a, 0, sizeof(a));
+    common(a, l);
     if (lp[l].nsolve > 0)
-      UKG_LAUNCH(UKG_K_SOLVE, st,
-                 (solve_kernel<<<grid(lp[l].nsolve, bs), bs, bs * pt_solve, st>>>(a, want_cov ? 1 : 0)));
+      UKG_LAUNCH(kSolve, st, (K.solve<<<grid(lp[l].nsolve, bs), bs, bs * pt_solve, st>>>(a, want_cov ? 1 : 0)));
+  }
+  /* ---- refinement sweeps (FP32 factors only) ---- */
+  if constexpr (sizeof(T) == sizeof(float)) {
+    const int requested = (int)((options >> 21) & 3u);
+    const int sweeps = P.refine ? (requested ? requested : 2) : 0;
+    double* dx = P.refine ? (double*)(B + P.o_dx) : nullptr;
+    for (int sw = 0; sw < sweeps; ++sw) {
+      {
+        Args<float, float> r;
+        memset(&r, 0, sizeof(r));
+        common(r, 0);
+        r.ce = eq0();
+        Soa<double> wE{(double*)(B + P.o_rE), P.S0}, zp{(double*)(B + P.o_rO), P.S0};
+        Soa<float> z0{(float*)(B + P.o_z[0]), std::max<int64_t>(lp[0].S, 1)};
+        UKG_LAUNCH(UKG_K_REFINE, st,
+                   (residual_kernel<<<grid(p->nsteps, br), br, br * pt_res, st>>>(r, raw, wE, zp, p->nsteps)));
+        UKG_LAUNCH(UKG_K_REFINE, st,
+                   (atr_kernel<<<grid(p->nsteps, 128), 128, 0, st>>>(r, raw, wE, zp, z0, p->nsteps)));
+      }
+      for (int l = 0; l < nlev; ++l) {
+        Args<float, float> a;
+        memset(&a, 0, sizeof(a));
+        common(a, l);
+        a.state = dx;
+        a.cov = nullptr;
+        Soa<float> zc{(float*)(B + P.o_z[l]), std::max<int64_t>(lp[l].S, 1)};
+        Soa<float> yc{(float*)(B + P.o_y[l]), std::max<int64_t>(lp[l].E, 1)};
+        if (lp[l].nsolve > 0)
+          UKG_LAUNCH(UKG_K_REFINE, st, (rt_even_kernel<<<grid(lp[l].nsolve, 128), 128, 0, st>>>(a, zc, yc)));
+        if (lp[l].npairs > 0 && l + 1 < nlev) {
+          Soa<float> zn{(float*)(B + P.o_z[l + 1]), std::max<int64_t>(lp[l + 1].S, 1)};
+          UKG_LAUNCH(UKG_K_REFINE, st, (rt_odd_kernel<<<grid(lp[l].npairs, 128), 128, 0, st>>>(a, zc, yc, zn)));
+        }
+        if (lp[l].ntail > 0) {
+          Soa<float> tmp{(float*)(B + P.o_tmp), std::max(T_, 1)};
+          UKG_LAUNCH(UKG_K_REFINE, st, (rt_base_kernel<<<grid(lp[l].ntail, 128), 128, 0, st>>>(a, zc, tmp)));
+        }
+      }
+      for (int l = nlev - 2; l >= 0; --l) {
+        Args<float, float> a;
+        memset(&a, 0, sizeof(a));
+        common(a, l);
+        a.state = dx;
+        a.cov = nullptr;
+        a.yrhs = Soa<float>{(float*)(B + P.o_y[l]), std::max<int64_t>(lp[l].E, 1)};
+        if (lp[l].nsolve > 0)
+          UKG_LAUNCH(UKG_K_REFINE, st, (K.solve<<<grid(lp[l].nsolve, bs), bs, bs * pt_solve, st>>>(a, 0)));
+      }
+      const int64_t cnt = p->nsteps * n;
+      UKG_LAUNCH(UKG_K_REFINE, st, (add_kernel<<<grid(cnt, 256), 256, 0, st>>>(p->state, dx, cnt)));
+    }
   }
   int hflag = 0;
   cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -873,14 +1320,16 @@ extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* 
 {
   if (p->nsteps == 0) return 0;
   const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
+  const bool fp32 = (options & KALMAN_GPU_FP32_REFINE) != 0;
   Plan P;
-  const size_t need = build_plan(p, want_cov, P, nullptr, 0);
+  const size_t need = build_plan(p, want_cov, fp32, fp32, P, nullptr, 0);
   if (need == 0) return ukg_set_error(KALMAN_GPU_EINVAL, "tracks longer than 2^%d steps", kMaxLevels - 1);
   tl_tab.resize(need);
-  build_plan(p, want_cov, P, tl_tab.data(), need);
+  build_plan(p, want_cov, fp32, fp32, P, tl_tab.data(), need);
   void* base = nullptr;
   if (int e = ensure_workspace(P.bytes, &base)) return e;
-  return run_plan(options, p, (cudaStream_t)cuda_stream, P, tl_tab.data(), (char*)base);
+  if (fp32) return run_plan<float>(options, p, (cudaStream_t)cuda_stream, P, tl_tab.data(), (char*)base);
+  return run_plan<double>(options, p, (cudaStream_t)cuda_stream, P, tl_tab.data(), (char*)base);
 }
 
 /* ---------------------------------------------------------------------------
@@ -945,17 +1394,18 @@ extern "C" int kalman_gpu_smooth_oddeven_noalloc(uint32_t options, const kalman_
   }
   const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
   Plan P;
-  const size_t need = build_plan(p, want_cov, P, nullptr, 0);
+  const size_t need = build_plan(p, want_cov, false, false, P, nullptr, 0);
   if (need == 0 || need > kNoallocTabEntries)
     return ukg_set_error(KALMAN_GPU_EINVAL, "the allocation-free entry point plans at most %zu table entries "
                          "(this problem needs %zu: too many tracks)", kNoallocTabEntries, need);
-  build_plan(p, want_cov, P, g_noalloc_tab, kNoallocTabEntries);
+  build_plan(p, want_cov, false, false, P, g_noalloc_tab, kNoallocTabEntries);
   if (P.bytes > (size_t)KALMAN_GPU_NOALLOC_SCRATCH_BYTES)
     return ukg_set_error(KALMAN_GPU_EINVAL, "this problem needs %zu bytes of scratch; the allocation-free entry "
                          "point has %zu (use kalman_gpu_smooth_oddeven_packed)", P.bytes,
                          (size_t)KALMAN_GPU_NOALLOC_SCRATCH_BYTES);
   const int prof = ukg_prof_pause(); /* profiling would create CUDA events */
-  const int status = run_plan(options, p, (cudaStream_t)cuda_stream, P, g_noalloc_tab, (char*)g_noalloc_addr[dev]);
+  const int status = run_plan<double>(options & ~(uint32_t)KALMAN_GPU_FP32_REFINE, p, (cudaStream_t)cuda_stream, P,
+                                      g_noalloc_tab, (char*)g_noalloc_addr[dev]);
   ukg_prof_resume(prof);
   return status;
 }

@@ -130,6 +130,45 @@ __global__ void fp64_fma_probe(double* out, int iters, double a, double b, int l
   if (s == 1234.5) out[blockIdx.x] = s; /* keeps the chains alive */
 }
 
+__global__ void fp32_fma_probe(float* out, int iters, float a, float b)
+{
+  float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+  }
+  float s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == 1234.5f) out[blockIdx.x] = s;
+}
+
+extern "C" double kalman_gpu_measure_fp32_tflops(void)
+{
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0.0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  float* out = nullptr;
+  if (cudaMalloc(&out, sizeof(float) * sms * 8) != cudaSuccess) return 0.0;
+  const int blocks = sms * 8, threads = 256, iters = 16384;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  fp32_fma_probe<<<blocks, threads>>>(out, iters, 0.9999f, 1e-4f);
+  float best = 1e30f;
+  for (int r = 0; r < 5; ++r) {
+    cudaEventRecord(a);
+    fp32_fma_probe<<<blocks, threads>>>(out, iters, 0.9999f, 1e-4f);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best) best = ms;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  return 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+}
+
 extern "C" double kalman_gpu_measure_fp64_tflops(int active_lanes)
 {
   if (active_lanes < 1 || active_lanes > 32) active_lanes = 32;

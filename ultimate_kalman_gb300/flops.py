@@ -142,3 +142,59 @@ def plan_flops_fast(track_lengths, n, m0, covariance=True):
     obs = np.full(int(ts[-1]), m0, dtype=np.int64)
     obs[ts[:-1][lengths > 0]] = n
     return plan_flops(lengths, obs, ts, n, covariance)
+
+
+def refine_flops(track_lengths, n, m, sweeps=2):
+    """One or more refinement sweeps: FP64 residual and A^T r per step (the
+    evolution rows of the step and of the next step, its observation rows),
+    then R^T y = z and R d = y over the levels in FP32."""
+    lengths = np.asarray(track_lengths, dtype=np.int64)
+    N = float(lengths.sum())
+    per_step = 2.0 * (6 * n * n + 2 * m * n)
+    evens = 0.0
+    L = lengths.copy()
+    while (L >= 2).any():
+        evens += float(np.where(L >= 2, (L + 1) // 2, 0).sum())
+        L = L // 2
+    per_even = 2.0 * (n * n / 2 + 2 * n * n + 2 * n * n + n * n / 2)
+    return sweeps * (N * per_step + evens * per_even)
+
+
+def plan_flops_fast_fp32(track_lengths, n, m0, sweeps=2):
+    """Kernel classes of the precision form (states only): FP64 weighing, FP32
+    factorization and back-substitution, refinement sweeps."""
+    f = plan_flops_fast(track_lengths, n, m0, covariance=False)
+    return {"weigh_kernel": f["weigh_kernel"], "fp32_pair_kernel": f["pair_kernel"], "tail_kernel": f["tail_kernel"],
+            "fp32_solve_kernel": f["solve_kernel"], "refine_kernel": refine_flops(track_lengths, n, m0, sweeps)}
+
+
+def plan_bytes_fast(track_lengths, n, mx, fp32=False, sweeps=2):
+    """Algorithmic DRAM bytes per kernel class for one smoothing (states only):
+    every input block read once, every output and intermediate written once
+    and read once.  Level-0 equations are FP64; levels and records are FP32
+    in the precision form."""
+    lengths = np.asarray(track_lengths, dtype=np.int64)
+    N = float(lengths.sum())
+    eqd = 2 * n * n + n + mx * n + mx
+    raw = 3 * n * n + n + mx * n + mx + mx * mx
+    t = 4.0 if fp32 else 8.0
+    out = {"weigh_kernel": N * (raw * 8 + 6 + eqd * 8 + 4)}
+    pair = solve = 0.0
+    L = lengths.copy()
+    level = 0
+    while (L >= 2).any():
+        pairs = float(np.where(L >= 2, L // 2, 0).sum())
+        evens = float(np.where(L >= 2, (L + 1) // 2, 0).sum())
+        size_in = 8.0 if level == 0 else t
+        pair += pairs * (2 * eqd * size_in + eqd * t + (3 * n * n + n) * t)
+        solve += evens * ((3 * n * n + n) * t + 3 * n * 8)
+        L = L // 2
+        level += 1
+    if fp32:
+        out["fp32_pair_kernel"] = pair
+        out["fp32_solve_kernel"] = solve
+        out["refine_kernel"] = sweeps * (N * (eqd * 8 + 4 * n * 8 + n * 4) + solve)
+    else:
+        out["pair_kernel"] = pair
+        out["solve_kernel"] = solve
+    return out

@@ -84,7 +84,7 @@ EXPORTED = [
     "kalman_gpu_last_status", "kalman_gpu_last_error", "kalman_gpu_clear_error",
     "kalman_gpu_smooth_oddeven_packed", "kalman_gpu_smooth_associative_packed", "kalman_gpu_smooth_tracks",
     "kalman_gpu_release", "kalman_gpu_profile_enable", "kalman_gpu_profile_read", "kalman_gpu_launch_count",
-    "kalman_gpu_measure_fp64_tflops", "kalman_gpu_smooth_oddeven_noalloc",
+    "kalman_gpu_measure_fp64_tflops", "kalman_gpu_measure_fp32_tflops", "kalman_gpu_smooth_oddeven_noalloc",
 ]
 
 _lib = None
@@ -118,6 +118,7 @@ def load(path=LIB_PATH):
     L.kalman_gpu_launch_count.restype = ctypes.c_int64
     L.kalman_gpu_measure_fp64_tflops.argtypes = [ctypes.c_int]
     L.kalman_gpu_measure_fp64_tflops.restype = ctypes.c_double
+    L.kalman_gpu_measure_fp32_tflops.restype = ctypes.c_double
     _lib = L
     return L
 
@@ -155,12 +156,16 @@ def measure_fp64_tflops(active_lanes=32):
     return load().kalman_gpu_measure_fp64_tflops(active_lanes)
 
 
-def options_for(algorithm, covariance=True, fp32_refine=False):
+def measure_fp32_tflops():
+    return load().kalman_gpu_measure_fp32_tflops()
+
+
+def options_for(algorithm, covariance=True, fp32_refine=False, sweeps=0):
     o = KALMAN_ALGORITHM_ODDEVEN if algorithm == "oddeven" else KALMAN_ALGORITHM_ASSOCIATIVE
     if not covariance:
         o |= KALMAN_NO_COVARIANCE
     if fp32_refine:
-        o |= KALMAN_GPU_FP32_REFINE
+        o |= KALMAN_GPU_FP32_REFINE | ((sweeps & 3) << 21)
     return o
 
 
@@ -196,11 +201,11 @@ class DeviceProblem:
     def input_bytes(self):
         return sum(a.numel() * a.element_size() for a in self.arrays.values())
 
-    def smooth(self, algorithm="oddeven", covariance=True, fp32_refine=False, stream=None, check=True):
+    def smooth(self, algorithm="oddeven", covariance=True, fp32_refine=False, stream=None, check=True, sweeps=0):
         L = load()
         torch = self.torch
         st = stream if stream is not None else torch.cuda.current_stream()
-        opts = options_for(algorithm, covariance and self.cov is not None, fp32_refine)
+        opts = options_for(algorithm, covariance and self.cov is not None, fp32_refine, sweeps)
         f = L.kalman_gpu_smooth_oddeven_packed if algorithm == "oddeven" else L.kalman_gpu_smooth_associative_packed
         status = f(opts, ctypes.byref(self.struct), ctypes.c_void_p(st.cuda_stream))
         if check:
@@ -215,13 +220,13 @@ class DeviceProblem:
         return X, S
 
 
-def smooth(P, algorithm="oddeven", covariance=True, fp32_refine=False, location="device"):
+def smooth(P, algorithm="oddeven", covariance=True, fp32_refine=False, location="device", sweeps=0):
     """Smooths a PackedProblem on the GPU; returns (states [N,n], covs [N,n,n] or None).
     location="device": inputs are copied to GPU memory first and the device
     entry point runs on them; "host": the library is handed host arrays."""
     if location == "device":
         D = DeviceProblem(P, covariance)
-        D.smooth(algorithm, covariance, fp32_refine)
+        D.smooth(algorithm, covariance, fp32_refine, sweeps=sweeps)
         return D.results()
     L = load()
     N, n = P.nsteps, P.n
@@ -237,7 +242,7 @@ def smooth(P, algorithm="oddeven", covariance=True, fp32_refine=False, location=
         setattr(s, f, arrs[f].ctypes.data)
     s.state = state.ctypes.data
     s.covariance = cov.ctypes.data if cov is not None else None
-    opts = options_for(algorithm, covariance, fp32_refine)
+    opts = options_for(algorithm, covariance, fp32_refine, sweeps)
     f = L.kalman_gpu_smooth_oddeven_packed if algorithm == "oddeven" else L.kalman_gpu_smooth_associative_packed
     _check(f(opts, ctypes.byref(s), None))
     if cov is not None:
@@ -348,9 +353,9 @@ def host_struct_from_tensors(P, arrays, state, cov):
     return s
 
 
-def smooth_struct(algorithm, s, covariance=True, fp32_refine=False, stream=None):
+def smooth_struct(algorithm, s, covariance=True, fp32_refine=False, stream=None, sweeps=0):
     """Runs a packed entry point on a prepared ProblemStruct."""
     L = load()
-    opts = options_for(algorithm, covariance, fp32_refine)
+    opts = options_for(algorithm, covariance, fp32_refine, sweeps)
     f = L.kalman_gpu_smooth_oddeven_packed if algorithm == "oddeven" else L.kalman_gpu_smooth_associative_packed
     _check(f(opts, ctypes.byref(s), ctypes.c_void_p(stream.cuda_stream) if stream is not None else None))
