@@ -363,6 +363,215 @@ __global__ void weigh_kernel(Args<T, T> a, RawDev raw, int64_t nsteps)
 }
 
 /* ---------------------------------------------------------------------------
+ * level 0, bulk-staged: the caller's blocks of 128 consecutive steps are
+ * contiguous, so each kind of matrix (K, H, F, c, C, G, o) is brought into
+ * shared memory by one bulk asynchronous copy (cp.async.bulk, the TMA engine)
+ * completing on an mbarrier, then every thread weighs its own step from there.
+ * Waits are bounded: a copy that does not complete sets flag bit 8.
+ * ------------------------------------------------------------------------ */
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity)
+{
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+/* polls the phase with a bound of about a second */
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+{
+  for (int it = 0; it < (1 << 23); ++it) {
+    if (mbar_test(bar, parity)) return true;
+    __nanosleep(100);
+  }
+  return false;
+}
+
+/* prepared weighing of one covariance factor in per-thread shared memory:
+ * 'C' Cholesky factor, 'U'/'F' lower triangle (L and reciprocal diagonal),
+ * 'W' the matrix itself (in L), 'w' the column (in dinv)                     */
+template <typename T, class V>
+__device__ bool prepare_weights(char type, const double* cov, int ldc, int rows, V L, V dinv)
+{
+  if (type == 'W') {
+    for (int j = 0; j < rows; ++j)
+      for (int i = 0; i < rows; ++i) L[j * rows + i] = (T)cov[j * ldc + i];
+    return true;
+  }
+  if (type == 'w') {
+    for (int i = 0; i < rows; ++i) dinv[i] = (T)cov[i];
+    return true;
+  }
+  if (type == 'U' || type == 'F') {
+    bool ok = true;
+    for (int j = 0; j < rows; ++j) {
+      for (int i = j; i < rows; ++i) L[j * rows + i] = (T)cov[j * ldc + i];
+      ok &= (L[j * rows + j] != T(0));
+      dinv[j] = T(1) / L[j * rows + j];
+    }
+    return ok;
+  }
+  for (int j = 0; j < rows; ++j) { /* 'C' */
+    T d = (T)cov[j * ldc + j];
+    for (int k = 0; k < j; ++k) d = fma(-L[k * rows + j], L[k * rows + j], d);
+    if (!(d > T(0))) return false;
+    d = sqrt(d);
+    const T r = T(1) / d;
+    L[j * rows + j] = d;
+    dinv[j] = r;
+    for (int i = j + 1; i < rows; ++i) {
+      T sum = (T)cov[j * ldc + i];
+      for (int k = 0; k < j; ++k) sum = fma(-L[k * rows + i], L[k * rows + j], sum);
+      L[j * rows + i] = sum * r;
+    }
+  }
+  return true;
+}
+
+template <typename T, class V>
+__device__ void apply_weights(char type, int rows, V L, V dinv, V col, V tmp)
+{
+  if (type == 'W') {
+    for (int i = 0; i < rows; ++i) {
+      T sum = T(0);
+      for (int j = 0; j < rows; ++j) sum = fma(L[j * rows + i], col[j], sum);
+      tmp[i] = sum;
+    }
+    for (int i = 0; i < rows; ++i) col[i] = tmp[i];
+  } else if (type == 'w') {
+    for (int i = 0; i < rows; ++i) col[i] *= dinv[i];
+  } else {
+    for (int j = 0; j < rows; ++j) {
+      const T xj = col[j] * dinv[j];
+      col[j] = xj;
+      for (int i = j + 1; i < rows; ++i) col[i] = fma(-xj, L[j * rows + i], col[i]);
+    }
+  }
+}
+
+constexpr int kWeighBS = 128;
+
+template <typename T>
+__global__ void __launch_bounds__(kWeighBS) weigh_staged_kernel(Args<T, T> a, RawDev raw, int64_t nsteps, int blk)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+  double* buf = reinterpret_cast<double*>(smem_raw + 16);
+  T* wsb = reinterpret_cast<T*>(smem_raw + 16 + (size_t)kWeighBS * blk * sizeof(double));
+  const int tid = threadIdx.x;
+  const int64_t g0 = (int64_t)blockIdx.x * kWeighBS, g = g0 + tid;
+  const int cnt = (int)((nsteps - g0) < kWeighBS ? (nsteps - g0) : kWeighBS);
+  const bool active = tid < cnt;
+  const int n = a.n, mx = a.mx, mm = raw.mmax;
+  PVc<T, kWeighBS> ws{wsb + tid};
+  PVc<T, kWeighBS> L = ws, dinv = ws + mx * mx, col = dinv + mx, tmp = col + mx;
+  if (tid == 0) mbar_init(bar);
+  __syncthreads();
+
+  int64_t q = 0, i = 0;
+  bool evol = false;
+  int m = 0;
+  char kt = 'C', ct = 'C';
+  if (active) {
+    const int t = find_track(a.track_start, a.ntracks, g);
+    i = g - a.track_start[t];
+    q = a.ct.slot[t] + i;
+    evol = i > 0;
+    kt = raw.K_type[g];
+    m = raw.obs_rows[g];
+    if (m < 0 || m > mm) {
+      m = 0;
+      atomicOr(a.flag, 4);
+    }
+    ct = raw.C_type[g];
+    if (evol && !valid_type(kt)) atomicOr(a.flag, 4);
+    if (m > 0 && !valid_type(ct)) atomicOr(a.flag, 4);
+    a.ce.m[q] = m;
+  }
+  bool bad = false;
+  uint32_t phase = 0;
+  /* parts: 0 K, 1 H, 2 F, 3 c, 4 C, 5 G, 6 o */
+  for (int part = 0; part < 7; ++part) {
+    const double* src;
+    int per;
+    switch (part) {
+      case 0: src = raw.K; per = n * n; break;
+      case 1: src = raw.H; per = n * n; break;
+      case 2: src = raw.F; per = n * n; break;
+      case 3: src = raw.c; per = n; break;
+      case 4: src = raw.C; per = mm * mm; break;
+      case 5: src = raw.G; per = mm * n; break;
+      default: src = raw.o; per = mm; break;
+    }
+    if (per == 0) continue;
+    const uint32_t bytes = (uint32_t)cnt * per * sizeof(double);
+    if (bytes % 16 == 0) { /* one bulk copy; both addresses are 16-byte aligned (g0 is a multiple of 128) */
+      if (tid == 0) bulk_load(buf, src + g0 * per, bytes, bar);
+      const bool ok = mbar_wait(bar, phase);
+      if (!__syncthreads_and(ok)) { /* the same decision in every thread */
+        if (tid == 0) atomicOr(a.flag, 8);
+        mbar_wait(bar, phase); /* give a late copy one more bounded chance before leaving */
+        return;
+      }
+      phase ^= 1;
+    } else {
+      for (int e = tid; e < cnt * per; e += kWeighBS) buf[e] = src[g0 * per + e];
+      __syncthreads();
+    }
+    if (active) {
+      const double* mine = buf + (size_t)tid * per;
+      if (part == 0 && evol) bad |= !prepare_weights<T>(kt, mine, n, n, L, dinv);
+      if ((part == 1 || part == 2 || part == 3) && evol) {
+        const int ncols = part == 3 ? 1 : n;
+        const T sgn = part == 2 ? T(-1) : T(1);
+        for (int cc = 0; cc < ncols; ++cc) {
+          for (int r = 0; r < n; ++r) col[r] = sgn * (T)mine[cc * n + r];
+          apply_weights<T>(kt, n, L, dinv, col, tmp);
+          for (int r = 0; r < n; ++r) {
+            if (part == 1) a.ce.H.at(cc * n + r, q) = col[r];
+            else if (part == 2) a.ce.F.at(cc * n + r, q) = col[r];
+            else a.ce.c.at(r, q) = col[r];
+          }
+        }
+      }
+      if (part == 4 && m > 0) bad |= !prepare_weights<T>(ct, mine, mm, m, L, dinv);
+      if ((part == 5 || part == 6) && m > 0) {
+        const int ncols = part == 6 ? 1 : n;
+        for (int cc = 0; cc < ncols; ++cc) {
+          for (int r = 0; r < m; ++r) col[r] = (T)mine[cc * mm + r];
+          apply_weights<T>(ct, m, L, dinv, col, tmp);
+          for (int r = 0; r < m; ++r) {
+            if (part == 5) a.ce.G.at(cc * mx + r, q) = col[r];
+            else a.ce.o.at(r, q) = col[r];
+          }
+        }
+      }
+    }
+    __syncthreads(); /* the buffer is refilled by the next part */
+  }
+  if (bad) atomicOr(a.flag, 1);
+}
+
+/* ---------------------------------------------------------------------------
  * forward elimination of one pair of a level
  * ------------------------------------------------------------------------ */
 /* NT, MT: compile-time n and mx (0: taken from the arguments); BS: the
@@ -465,6 +674,245 @@ __global__ void __launch_bounds__(BS ? BS : 1024) pair_kernel(Args<T, TI> a, int
       for (int i = 0; i < n; ++i) N.H.at(q * n + i, sn) = col[n + i];
     }
   }
+}
+
+/* ---------------------------------------------------------------------------
+ * FP32 pair elimination with every block in registers.  The row counts of
+ * stages A (m_j + n) and C (m_j + m_{j+1}) are dispatched at run time to
+ * instantiations in which every loop bound is a compile-time constant, so the
+ * pivot block P[col][row], the reflector scalars and the streamed column are
+ * register arrays.  Same arithmetic as pair_kernel.
+ * ------------------------------------------------------------------------ */
+template <int R, int C>
+__device__ __forceinline__ void hh_reg(float (&P)[C][R], float (&tau)[C])
+{
+#pragma unroll
+  for (int k = 0; k < C; ++k) {
+    tau[k] = 0.0f;
+    if (k >= R) continue;
+    const float alpha = P[k][k];
+    float tail = 0.0f;
+#pragma unroll
+    for (int i = k + 1; i < R; ++i) tail = fmaf(P[k][i], P[k][i], tail);
+    if (tail != 0.0f) {
+      const float beta = -copysignf(sqrtf(fmaf(alpha, alpha, tail)), alpha);
+      const float amb = alpha - beta;
+      const float inv = 1.0f / (beta * amb);
+      const float t = -(amb * amb) * inv;
+      const float scale = beta * inv;
+#pragma unroll
+      for (int i = k + 1; i < R; ++i) P[k][i] *= scale;
+      P[k][k] = beta;
+#pragma unroll
+      for (int j = k + 1; j < C; ++j) {
+        float d = P[j][k];
+#pragma unroll
+        for (int i = k + 1; i < R; ++i) d = fmaf(P[k][i], P[j][i], d);
+        d *= t;
+        P[j][k] -= d;
+#pragma unroll
+        for (int i = k + 1; i < R; ++i) P[j][i] = fmaf(-d, P[k][i], P[j][i]);
+      }
+      tau[k] = t;
+    }
+  }
+}
+
+template <int R, int C>
+__device__ __forceinline__ void apply_reg(const float (&P)[C][R], const float (&tau)[C], float (&col)[R])
+{
+#pragma unroll
+  for (int k = 0; k < C; ++k) {
+    if (k >= R) continue;
+    const float t = tau[k];
+    float d = col[k];
+#pragma unroll
+    for (int i = k + 1; i < R; ++i) d = fmaf(P[k][i], col[i], d);
+    d *= t;
+    col[k] -= d;
+#pragma unroll
+    for (int i = k + 1; i < R; ++i) col[i] = fmaf(-d, P[k][i], col[i]);
+  }
+}
+
+struct PairIdx {
+  int64_t sj, sj1, sn, se;
+};
+
+/* stage A with RA = m_j + N rows: pivot [G_j; F_{j+1}], rhs [o_j; c_{j+1}] */
+template <int N, int MX, int RA>
+__device__ __forceinline__ void reg_stage_a(const Args<float, float>& a, const PairIdx& x)
+{
+  constexpr int MJ = RA - N;
+  const Eq<float>& C = a.ce;
+  const Eq<float>& Nx = a.ne;
+  const Rec<float>& Rr = a.cr;
+  float P[N][RA], v[RA], tau[N];
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+#pragma unroll
+    for (int i = 0; i < MJ; ++i) P[q][i] = C.G.at(q * MX + i, x.sj);
+#pragma unroll
+    for (int i = 0; i < N; ++i) P[q][MJ + i] = C.F.at(q * N + i, x.sj1);
+  }
+#pragma unroll
+  for (int i = 0; i < MJ; ++i) v[i] = C.o.at(i, x.sj);
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[MJ + i] = C.c.at(i, x.sj1);
+  hh_reg<RA, N>(P, tau);
+  apply_reg<RA, N>(P, tau, v);
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < N; ++i) Rr.R.at(q * N + i, x.se) = (i <= q) ? P[q][i] : 0.0f;
+#pragma unroll
+  for (int i = 0; i < N; ++i) Rr.rhs.at(i, x.se) = v[i];
+#pragma unroll
+  for (int i = 0; i < MJ; ++i) Nx.o.at(i, x.sn) = v[N + i];
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    float col[RA];
+#pragma unroll
+    for (int i = 0; i < MJ; ++i) col[i] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < N; ++i) col[MJ + i] = C.H.at(q * N + i, x.sj1);
+    apply_reg<RA, N>(P, tau, col);
+#pragma unroll
+    for (int i = 0; i < N; ++i) Rr.Y.at(q * N + i, x.se) = col[i];
+#pragma unroll
+    for (int i = 0; i < MJ; ++i) Nx.G.at(q * MX + i, x.sn) = col[N + i];
+  }
+}
+
+/* stage C with RC = m_j + m_{j+1} rows: pivot [H~_{j+1}; G_{j+1}] */
+template <int N, int MX, int RC>
+__device__ __forceinline__ void reg_stage_c(const Args<float, float>& a, const PairIdx& x, int mj)
+{
+  const Eq<float>& C = a.ce;
+  const Eq<float>& Nx = a.ne;
+  float P[N][RC], v[RC], tau[N];
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < RC; ++i) P[q][i] = i < mj ? Nx.G.at(q * MX + i, x.sn) : C.G.at(q * MX + (i - mj), x.sj1);
+#pragma unroll
+  for (int i = 0; i < RC; ++i) v[i] = i < mj ? Nx.o.at(i, x.sn) : C.o.at(i - mj, x.sj1);
+  hh_reg<RC, N>(P, tau);
+  apply_reg<RC, N>(P, tau, v);
+  constexpr int G = RC < N ? RC : N;
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < G; ++i) Nx.G.at(q * MX + i, x.sn) = (i <= q) ? P[q][i] : 0.0f;
+#pragma unroll
+  for (int i = 0; i < G; ++i) Nx.o.at(i, x.sn) = v[i];
+  Nx.m[x.sn] = G;
+}
+
+/* stage B: pivot [H_j; R~_j] (2N rows) */
+template <int N, int MX>
+__device__ __forceinline__ void reg_stage_b(const Args<float, float>& a, const PairIdx& x)
+{
+  constexpr int R2 = 2 * N;
+  const Eq<float>& C = a.ce;
+  const Eq<float>& Nx = a.ne;
+  const Rec<float>& Rr = a.cr;
+  float P[N][R2], v[R2], tau[N];
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      P[q][i] = C.H.at(q * N + i, x.sj);
+      P[q][N + i] = Rr.R.at(q * N + i, x.se);
+    }
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    v[i] = C.c.at(i, x.sj);
+    v[N + i] = Rr.rhs.at(i, x.se);
+  }
+  hh_reg<R2, N>(P, tau);
+  apply_reg<R2, N>(P, tau, v);
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < N; ++i) Rr.R.at(q * N + i, x.se) = (i <= q) ? P[q][i] : 0.0f;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    Rr.rhs.at(i, x.se) = v[i];
+    Nx.c.at(i, x.sn) = v[N + i];
+  }
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    float col[R2];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      col[i] = C.F.at(q * N + i, x.sj);
+      col[N + i] = 0.0f;
+    }
+    apply_reg<R2, N>(P, tau, col);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Rr.Ft.at(q * N + i, x.se) = col[i];
+      Nx.F.at(q * N + i, x.sn) = col[N + i];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    float col[R2];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      col[i] = 0.0f;
+      col[N + i] = Rr.Y.at(q * N + i, x.se);
+    }
+    apply_reg<R2, N>(P, tau, col);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Rr.Y.at(q * N + i, x.se) = col[i];
+      Nx.H.at(q * N + i, x.sn) = col[N + i];
+    }
+  }
+}
+
+template <int N, int MX, int RA = N>
+__device__ __forceinline__ void reg_dispatch_a(int ra, const Args<float, float>& a, const PairIdx& x)
+{
+  if constexpr (RA <= N + MX) {
+    if (ra == RA) reg_stage_a<N, MX, RA>(a, x);
+    else reg_dispatch_a<N, MX, RA + 1>(ra, a, x);
+  }
+}
+
+template <int N, int MX, int RC = 1>
+__device__ __forceinline__ void reg_dispatch_c(int rc, const Args<float, float>& a, const PairIdx& x, int mj)
+{
+  if constexpr (RC <= 2 * MX) {
+    if (rc == RC) reg_stage_c<N, MX, RC>(a, x, mj);
+    else reg_dispatch_c<N, MX, RC + 1>(rc, a, x, mj);
+  }
+}
+
+template <int N, int MX>
+__global__ void __launch_bounds__(128) pair_reg_kernel(Args<float, float> a, int)
+{
+  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= a.ct.npairs) return;
+  const int t = find_track(a.ct.pair, a.ntracks, item);
+  const int64_t p = item - a.ct.pair[t];
+  PairIdx x;
+  x.sj = a.ct.slot[t] + 2 * p;
+  x.sj1 = x.sj + 1;
+  x.sn = a.nt.slot[t] + p;
+  x.se = a.ct.solve[t] + p;
+  const int mj = a.ce.m[x.sj], mj1 = a.ce.m[x.sj1];
+  reg_dispatch_a<N, MX>(mj + N, a, x);
+  if (mj + mj1 == 0) a.ne.m[x.sn] = 0;
+  else reg_dispatch_c<N, MX>(mj + mj1, a, x, mj);
+  if (p == 0) {
+#pragma unroll
+    for (int e = 0; e < N * N; ++e) a.cr.Ft.at(e, x.se) = 0.0f;
+    return;
+  }
+  reg_stage_b<N, MX>(a, x);
 }
 
 /* ---------------------------------------------------------------------------
@@ -1060,6 +1508,15 @@ template <typename T>
 Kernels<T> choose_kernels(int n, int mx)
 {
   Kernels<T> k;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if (n == mx && (n == 6 || n == 4)) {
+      k.pair = n == 6 ? pair_reg_kernel<6, 6> : pair_reg_kernel<4, 4>;
+      k.solve = n == 6 ? solve_kernel<T, 6, 64> : solve_kernel<T, 4, 64>;
+      k.bp = 128;
+      k.bs = 64;
+      return k;
+    }
+  }
   if (n == mx && n == 6) {
     k.pair = pair_kernel<T, T, 6, 6, 128>;
     k.solve = solve_kernel<T, 6, 64>;
@@ -1137,6 +1594,16 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
   const int rmax = 2 * mx;
   const size_t ts = sizeof(T);
   const size_t pt_weigh = (size_t)(mx * mx + 3 * mx) * ts;
+  const int mmx = p->mmax;
+  const int blk = std::max(std::max(n * n, mmx * mmx), std::max(mmx * n, 1));
+  const size_t weigh_smem = 16 + (size_t)kWeighBS * blk * sizeof(double) + (size_t)kWeighBS * pt_weigh;
+  int optin = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  /* bulk copies need 16-byte aligned sources */
+  const uintptr_t align_bits = (uintptr_t)p->H | (uintptr_t)p->F | (uintptr_t)p->c | (uintptr_t)p->K |
+                               (uintptr_t)p->G | (uintptr_t)p->o | (uintptr_t)p->C;
+  const bool staged = sizeof(T) == sizeof(float) && weigh_smem <= (size_t)optin && (align_bits & 15) == 0;
   const size_t pt_pair = (size_t)(rmax * (n + 1) + n + rmax) * ts;
   const size_t pt_tail = (size_t)(mx * (n + 1) + 2 * n * (2 * n + 1) + 2 * n * (n + 1) + 2 * n + nn) * ts;
   const size_t pt_solve = (size_t)(4 * nn + 4 * n) * ts;
@@ -1150,6 +1617,8 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
   if (K.bp) bp = K.bp;
   if (K.bs) bs = K.bs;
   cudaFuncSetAttribute(weigh_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bw * pt_weigh));
+  if (staged)
+    cudaFuncSetAttribute(weigh_staged_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)weigh_smem);
   cudaFuncSetAttribute(K.pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bp * pt_pair));
   cudaFuncSetAttribute(tail_kernel<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bt * pt_tail));
   cudaFuncSetAttribute(K.solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bs * pt_solve));
@@ -1172,8 +1641,13 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
     w.ntracks = T_;
     w.track_start = dtab + P.off_ts;
     w.flag = dflag;
-    UKG_LAUNCH(UKG_K_WEIGH, st,
-               (weigh_kernel<T><<<grid(p->nsteps, bw), bw, bw * pt_weigh, st>>>(w, raw, p->nsteps)));
+    if (staged)
+      UKG_LAUNCH(UKG_K_WEIGH, st,
+                 (weigh_staged_kernel<T><<<grid(p->nsteps, kWeighBS), kWeighBS, weigh_smem, st>>>(w, raw, p->nsteps,
+                                                                                                   blk)));
+    else
+      UKG_LAUNCH(UKG_K_WEIGH, st,
+                 (weigh_kernel<T><<<grid(p->nsteps, bw), bw, bw * pt_weigh, st>>>(w, raw, p->nsteps)));
   }
   auto common = [&](auto& a, int l) {
     a.ct = tables(l);
@@ -1223,9 +1697,9 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
         r.ce = eq0();
         Soa<double> wE{(double*)(B + P.o_rE), P.S0}, zp{(double*)(B + P.o_rO), P.S0};
         Soa<float> z0{(float*)(B + P.o_z[0]), std::max<int64_t>(lp[0].S, 1)};
-        UKG_LAUNCH(UKG_K_REFINE, st,
+        UKG_LAUNCH(UKG_K_RESID, st,
                    (residual_kernel<<<grid(p->nsteps, br), br, br * pt_res, st>>>(r, raw, wE, zp, p->nsteps)));
-        UKG_LAUNCH(UKG_K_REFINE, st,
+        UKG_LAUNCH(UKG_K_RESID, st,
                    (atr_kernel<<<grid(p->nsteps, 128), 128, 0, st>>>(r, raw, wE, zp, z0, p->nsteps)));
       }
       for (int l = 0; l < nlev; ++l) {
@@ -1237,14 +1711,14 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
         Soa<float> zc{(float*)(B + P.o_z[l]), std::max<int64_t>(lp[l].S, 1)};
         Soa<float> yc{(float*)(B + P.o_y[l]), std::max<int64_t>(lp[l].E, 1)};
         if (lp[l].nsolve > 0)
-          UKG_LAUNCH(UKG_K_REFINE, st, (rt_even_kernel<<<grid(lp[l].nsolve, 128), 128, 0, st>>>(a, zc, yc)));
+          UKG_LAUNCH(UKG_K_RT, st, (rt_even_kernel<<<grid(lp[l].nsolve, 128), 128, 0, st>>>(a, zc, yc)));
         if (lp[l].npairs > 0 && l + 1 < nlev) {
           Soa<float> zn{(float*)(B + P.o_z[l + 1]), std::max<int64_t>(lp[l + 1].S, 1)};
-          UKG_LAUNCH(UKG_K_REFINE, st, (rt_odd_kernel<<<grid(lp[l].npairs, 128), 128, 0, st>>>(a, zc, yc, zn)));
+          UKG_LAUNCH(UKG_K_RT, st, (rt_odd_kernel<<<grid(lp[l].npairs, 128), 128, 0, st>>>(a, zc, yc, zn)));
         }
         if (lp[l].ntail > 0) {
           Soa<float> tmp{(float*)(B + P.o_tmp), std::max(T_, 1)};
-          UKG_LAUNCH(UKG_K_REFINE, st, (rt_base_kernel<<<grid(lp[l].ntail, 128), 128, 0, st>>>(a, zc, tmp)));
+          UKG_LAUNCH(UKG_K_RT, st, (rt_base_kernel<<<grid(lp[l].ntail, 128), 128, 0, st>>>(a, zc, tmp)));
         }
       }
       for (int l = nlev - 2; l >= 0; --l) {
@@ -1255,7 +1729,7 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
         a.cov = nullptr;
         a.yrhs = Soa<float>{(float*)(B + P.o_y[l]), std::max<int64_t>(lp[l].E, 1)};
         if (lp[l].nsolve > 0)
-          UKG_LAUNCH(UKG_K_REFINE, st, (K.solve<<<grid(lp[l].nsolve, bs), bs, bs * pt_solve, st>>>(a, 0)));
+          UKG_LAUNCH(UKG_K_RSOLVE, st, (K.solve<<<grid(lp[l].nsolve, bs), bs, bs * pt_solve, st>>>(a, 0)));
       }
       const int64_t cnt = p->nsteps * n;
       UKG_LAUNCH(UKG_K_REFINE, st, (add_kernel<<<grid(cnt, 256), 256, 0, st>>>(p->state, dx, cnt)));
@@ -1267,6 +1741,7 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) return ukg_set_error(KALMAN_GPU_ECUDA, "odd-even smoother: %s", cudaGetErrorString(e));
   ukg_prof_collect();
+  if (hflag & 8) return ukg_set_error(KALMAN_GPU_ECUDA, "a bulk copy into shared memory did not complete in time");
   if (hflag & 4) return ukg_set_error(KALMAN_GPU_EINVAL, "malformed input: observation rows outside [0, mmax] or an "
                                      "unknown covariance type");
   if (hflag & 1) return ukg_set_error(KALMAN_GPU_ESINGULAR, "a covariance factor is not positive definite");

@@ -15,6 +15,9 @@ enum {
   UKG_K_REFINE,
   UKG_K_PAIR32,
   UKG_K_SOLVE32,
+  UKG_K_RESID,
+  UKG_K_RT,
+  UKG_K_RSOLVE,
   UKG_K_COUNT
 };
 
