@@ -51,6 +51,8 @@
  */
 #include <cuda_runtime.h>
 
+#include "df64.cuh"
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -252,12 +254,12 @@ __device__ void weigh_column(char type, const double* cov, int ldc, int rows, PV
   if (type == 'W') {
     for (int i = 0; i < rows; ++i) {
       T s = T(0);
-      for (int j = 0; j < rows; ++j) s = fma((T)cov[(int64_t)j * ldc + i], col[j], s);
+      for (int j = 0; j < rows; ++j) s = fma(ukg_df::narrow<T>(cov[(int64_t)j * ldc + i]), col[j], s);
       tmp[i] = s;
     }
     for (int i = 0; i < rows; ++i) col[i] = tmp[i];
   } else if (type == 'w') {
-    for (int i = 0; i < rows; ++i) col[i] *= (T)cov[i];
+    for (int i = 0; i < rows; ++i) col[i] *= ukg_df::narrow<T>(cov[i]);
   } else { /* forward substitution with the lower-triangular factor */
     for (int j = 0; j < rows; ++j) {
       const T xj = col[j] * dinv[j];
@@ -280,7 +282,7 @@ __device__ bool lower_factor(char type, const double* cov, int ldc, int rows, PV
   if (type == 'U' || type == 'F') {
     bool ok = true;
     for (int j = 0; j < rows; ++j) {
-      for (int i = j; i < rows; ++i) L[j * rows + i] = (T)cov[(int64_t)j * ldc + i];
+      for (int i = j; i < rows; ++i) L[j * rows + i] = ukg_df::narrow<T>(cov[(int64_t)j * ldc + i]);
       const T d = L[j * rows + j];
       ok &= (d != T(0));
       dinv[j] = T(1) / d;
@@ -289,7 +291,7 @@ __device__ bool lower_factor(char type, const double* cov, int ldc, int rows, PV
   }
   if (type != 'C') return true;
   for (int j = 0; j < rows; ++j) {
-    T d = (T)cov[(int64_t)j * ldc + j];
+    T d = ukg_df::narrow<T>(cov[(int64_t)j * ldc + j]);
     for (int k = 0; k < j; ++k) d = fma(-L[k * rows + j], L[k * rows + j], d);
     if (!(d > T(0))) return false;
     d = sqrt(d);
@@ -297,7 +299,7 @@ __device__ bool lower_factor(char type, const double* cov, int ldc, int rows, PV
     L[j * rows + j] = d;
     dinv[j] = r;
     for (int i = j + 1; i < rows; ++i) {
-      T s = (T)cov[(int64_t)j * ldc + i];
+      T s = ukg_df::narrow<T>(cov[(int64_t)j * ldc + i]);
       for (int k = 0; k < j; ++k) s = fma(-L[k * rows + i], L[k * rows + j], s);
       L[j * rows + i] = s * r;
     }
@@ -329,7 +331,7 @@ __global__ void weigh_kernel(Args<T, T> a, RawDev raw, int64_t nsteps)
       const double* src = part < n ? raw.H + g * nn + (int64_t)part * n
                         : part < 2 * n ? raw.F + g * nn + (int64_t)(part - n) * n : raw.c + g * n;
       const T sgn = (part >= n && part < 2 * n) ? T(-1) : T(1);
-      for (int r = 0; r < n; ++r) col[r] = sgn * (T)src[r];
+      for (int r = 0; r < n; ++r) col[r] = sgn * ukg_df::narrow<T>(src[r]);
       weigh_column(kt, K, n, n, L, dinv, col, tmp);
       for (int r = 0; r < n; ++r) {
         if (part < n) a.ce.H.at(part * n + r, q) = col[r];
@@ -351,7 +353,7 @@ __global__ void weigh_kernel(Args<T, T> a, RawDev raw, int64_t nsteps)
     bad |= !lower_factor(ct, C, mm, m, L, dinv);
     for (int part = 0; part <= n; ++part) { /* n columns of G, then o */
       const double* src = part < n ? raw.G + g * (int64_t)mm * n + (int64_t)part * mm : raw.o + g * mm;
-      for (int r = 0; r < m; ++r) col[r] = (T)src[r];
+      for (int r = 0; r < m; ++r) col[r] = ukg_df::narrow<T>(src[r]);
       weigh_column(ct, C, mm, m, L, dinv, col, tmp);
       for (int r = 0; r < m; ++r) {
         if (part < n) a.ce.G.at(part * mx + r, q) = col[r];
@@ -414,24 +416,24 @@ __device__ bool prepare_weights(char type, const double* cov, int ldc, int rows,
 {
   if (type == 'W') {
     for (int j = 0; j < rows; ++j)
-      for (int i = 0; i < rows; ++i) L[j * rows + i] = (T)cov[j * ldc + i];
+      for (int i = 0; i < rows; ++i) L[j * rows + i] = ukg_df::narrow<T>(cov[j * ldc + i]);
     return true;
   }
   if (type == 'w') {
-    for (int i = 0; i < rows; ++i) dinv[i] = (T)cov[i];
+    for (int i = 0; i < rows; ++i) dinv[i] = ukg_df::narrow<T>(cov[i]);
     return true;
   }
   if (type == 'U' || type == 'F') {
     bool ok = true;
     for (int j = 0; j < rows; ++j) {
-      for (int i = j; i < rows; ++i) L[j * rows + i] = (T)cov[j * ldc + i];
+      for (int i = j; i < rows; ++i) L[j * rows + i] = ukg_df::narrow<T>(cov[j * ldc + i]);
       ok &= (L[j * rows + j] != T(0));
       dinv[j] = T(1) / L[j * rows + j];
     }
     return ok;
   }
   for (int j = 0; j < rows; ++j) { /* 'C' */
-    T d = (T)cov[j * ldc + j];
+    T d = ukg_df::narrow<T>(cov[j * ldc + j]);
     for (int k = 0; k < j; ++k) d = fma(-L[k * rows + j], L[k * rows + j], d);
     if (!(d > T(0))) return false;
     d = sqrt(d);
@@ -439,7 +441,7 @@ __device__ bool prepare_weights(char type, const double* cov, int ldc, int rows,
     L[j * rows + j] = d;
     dinv[j] = r;
     for (int i = j + 1; i < rows; ++i) {
-      T sum = (T)cov[j * ldc + i];
+      T sum = ukg_df::narrow<T>(cov[j * ldc + i]);
       for (int k = 0; k < j; ++k) sum = fma(-L[k * rows + i], L[k * rows + j], sum);
       L[j * rows + i] = sum * r;
     }
@@ -544,7 +546,7 @@ __global__ void __launch_bounds__(kWeighBS) weigh_staged_kernel(Args<T, T> a, Ra
         const int ncols = part == 3 ? 1 : n;
         const T sgn = part == 2 ? T(-1) : T(1);
         for (int cc = 0; cc < ncols; ++cc) {
-          for (int r = 0; r < n; ++r) col[r] = sgn * (T)mine[cc * n + r];
+          for (int r = 0; r < n; ++r) col[r] = sgn * ukg_df::narrow<T>(mine[cc * n + r]);
           apply_weights<T>(kt, n, L, dinv, col, tmp);
           for (int r = 0; r < n; ++r) {
             if (part == 1) a.ce.H.at(cc * n + r, q) = col[r];
@@ -557,11 +559,229 @@ __global__ void __launch_bounds__(kWeighBS) weigh_staged_kernel(Args<T, T> a, Ra
       if ((part == 5 || part == 6) && m > 0) {
         const int ncols = part == 6 ? 1 : n;
         for (int cc = 0; cc < ncols; ++cc) {
-          for (int r = 0; r < m; ++r) col[r] = (T)mine[cc * mm + r];
+          for (int r = 0; r < m; ++r) col[r] = ukg_df::narrow<T>(mine[cc * mm + r]);
           apply_weights<T>(ct, m, L, dinv, col, tmp);
           for (int r = 0; r < m; ++r) {
             if (part == 5) a.ce.G.at(cc * mx + r, q) = col[r];
             else a.ce.o.at(r, q) = col[r];
+          }
+        }
+      }
+    }
+    __syncthreads(); /* the buffer is refilled by the next part */
+  }
+  if (bad) atomicOr(a.flag, 1);
+}
+
+/* ---------------------------------------------------------------------------
+ * Level-0 weighing in double-float arithmetic (FP32 factors with refinement).
+ * The same weighing as weigh_kernel, each weighed entry computed to about 47
+ * bits and stored as its FP32 high part (the level-0 arrays the FP32
+ * factorization reads) and FP32 low part (`lo`, read by the refinement
+ * residual).  Parts are staged as in weigh_staged_kernel; the covariance
+ * factor of a part lives in registers (compile-time N and MX).
+ * ------------------------------------------------------------------------ */
+template <int R>
+struct DfWeights {
+  ukg_df::df v[R * R]; /* the weighing V, column-major: V(i, j) at v[j * R + i] */
+  bool full;           /* 'W': every entry; otherwise V is lower triangular */
+  int rows;
+
+  /* V for the covariance factor (cov: entry (i, j) at cov[j * ld + i], the
+   * first nrows rows and columns): 'W' the matrix, 'w' its diagonal, 'C'
+   * chol(cov)^{-1}, 'U'/'F' tril(cov)^{-1}.  False: not positive definite or
+   * a zero pivot.  One code path for all types keeps the kernel small.       */
+  __device__ __forceinline__ bool prepare(char t, const double* cov, int ld, int nrows)
+  {
+    using namespace ukg_df;
+    rows = nrows;
+    full = t == 'W';
+    const bool diag = t == 'w', tri_in = t == 'U' || t == 'F', chol = t == 'C';
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        df e = make(i == j && !(full || diag || tri_in || chol) ? 1.0f : 0.0f);
+        if (i < rows && j < rows) {
+          if (full || ((tri_in || chol) && i >= j)) e = split(cov[j * ld + i]);
+          else if (diag && i == j) e = split(cov[i]);
+        }
+        v[j * R + i] = e;
+      }
+    if (!(tri_in || chol)) return true;
+    bool ok = true;
+    if (chol) { /* lower Cholesky factor in place */
+#pragma unroll
+      for (int j = 0; j < R; ++j) {
+        if (j >= rows) continue;
+        df d = v[j * R + j];
+#pragma unroll
+        for (int k = 0; k < j; ++k) d = ukg_df::fma(neg(v[k * R + j]), v[k * R + j], d);
+        if (!(d.hi > 0.0f)) {
+          ok = false;
+          d = make(1.0f);
+        }
+        const df l = ukg_df::sqrt(d), r = rcp(l);
+        v[j * R + j] = l;
+#pragma unroll
+        for (int i = j + 1; i < R; ++i) {
+          if (i >= rows) continue;
+          df sm = v[j * R + i];
+#pragma unroll
+          for (int k = 0; k < j; ++k) sm = ukg_df::fma(neg(v[k * R + i]), v[k * R + j], sm);
+          v[j * R + i] = mul(sm, r);
+        }
+      }
+    }
+    /* L^{-1} in place, last column first: column j of the inverse is
+     * -(1/L_jj) Linv[j+1:, j+1:] L[j+1:, j] below the diagonal 1/L_jj */
+#pragma unroll
+    for (int j = R - 1; j >= 0; --j) {
+      if (j >= rows) continue;
+      ok &= v[j * R + j].hi != 0.0f;
+      const df ajj = rcp(v[j * R + j]), najj = neg(ajj);
+      df t[R];
+#pragma unroll
+      for (int i = j + 1; i < R; ++i) {
+        df sm = make(0.0f);
+#pragma unroll
+        for (int k = j + 1; k <= i; ++k)
+          if (i < rows) sm = ukg_df::fma(v[k * R + i], v[j * R + k], sm);
+        t[i] = mul(sm, najj);
+      }
+#pragma unroll
+      for (int i = j + 1; i < R; ++i)
+        if (i < rows) v[j * R + i] = t[i];
+      v[j * R + j] = ajj;
+    }
+    return ok;
+  }
+
+  /* col <- V col on the first `rows` entries */
+  __device__ __forceinline__ void apply(ukg_df::df (&col)[R]) const
+  {
+    using namespace ukg_df;
+    df t[R];
+#pragma unroll
+    for (int i = R - 1; i >= 0; --i) {
+      df sm = make(0.0f);
+#pragma unroll
+      for (int j = 0; j <= i; ++j)
+        if (i < rows) sm = ukg_df::fma(v[j * R + i], col[j], sm);
+      t[i] = sm;
+    }
+    if (full) {
+#pragma unroll
+      for (int i = 0; i < R; ++i)
+#pragma unroll
+        for (int j = i + 1; j < R; ++j)
+          if (j < rows) t[i] = ukg_df::fma(v[j * R + i], col[j], t[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < R; ++i) col[i] = t[i];
+  }
+};
+
+template <int N, int MX>
+__global__ void __launch_bounds__(kWeighBS) weigh_df_kernel(Args<float, float> a, Eq<float> lo, RawDev raw,
+                                                            int64_t nsteps, int bulk)
+{
+  using namespace ukg_df;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+  double* buf = reinterpret_cast<double*>(smem_raw + 16);
+  const int tid = threadIdx.x;
+  const int64_t g0 = (int64_t)blockIdx.x * kWeighBS, g = g0 + tid;
+  const int cnt = (int)((nsteps - g0) < kWeighBS ? (nsteps - g0) : kWeighBS);
+  const bool active = tid < cnt;
+  const int mm = raw.mmax;
+  if (tid == 0) mbar_init(bar);
+  __syncthreads();
+
+  int64_t q = 0, i = 0;
+  bool evol = false;
+  int m = 0;
+  char kt = 'C', ct = 'C';
+  if (active) {
+    const int t = find_track(a.track_start, a.ntracks, g);
+    i = g - a.track_start[t];
+    q = a.ct.slot[t] + i;
+    evol = i > 0;
+    kt = raw.K_type[g];
+    m = raw.obs_rows[g];
+    if (m < 0 || m > mm) {
+      m = 0;
+      atomicOr(a.flag, 4);
+    }
+    ct = raw.C_type[g];
+    if (evol && !valid_type(kt)) atomicOr(a.flag, 4);
+    if (m > 0 && !valid_type(ct)) atomicOr(a.flag, 4);
+    a.ce.m[q] = m;
+  }
+  bool bad = false;
+  uint32_t phase = 0;
+  DfWeights<MX> V;
+  /* parts: 0 K, 1 H, 2 F, 3 c, 4 C, 5 G, 6 o */
+  for (int part = 0; part < 7; ++part) {
+    const double* src;
+    int per;
+    switch (part) {
+      case 0: src = raw.K; per = N * N; break;
+      case 1: src = raw.H; per = N * N; break;
+      case 2: src = raw.F; per = N * N; break;
+      case 3: src = raw.c; per = N; break;
+      case 4: src = raw.C; per = mm * mm; break;
+      case 5: src = raw.G; per = mm * N; break;
+      default: src = raw.o; per = mm; break;
+    }
+    if (per == 0) continue;
+    const uint32_t bytes = (uint32_t)cnt * per * sizeof(double);
+    if (bulk && bytes % 16 == 0) { /* one bulk copy; both addresses are 16-byte aligned (g0 is a multiple of 128) */
+      if (tid == 0) bulk_load(buf, src + g0 * per, bytes, bar);
+      const bool ok = mbar_wait(bar, phase);
+      if (!__syncthreads_and(ok)) { /* the same decision in every thread */
+        if (tid == 0) atomicOr(a.flag, 8);
+        mbar_wait(bar, phase); /* give a late copy one more bounded chance before leaving */
+        return;
+      }
+      phase ^= 1;
+    } else {
+      for (int e = tid; e < cnt * per; e += kWeighBS) buf[e] = src[g0 * per + e];
+      __syncthreads();
+    }
+    if (active) {
+      const double* mine = buf + (size_t)tid * per;
+      const bool evpart = part <= 3;
+      const int rows = evpart ? N : m, ld = evpart ? N : mm;
+      if ((evpart ? evol : m > 0)) {
+        if (part == 0 || part == 4) {
+          bad |= !V.prepare(part == 0 ? kt : ct, mine, ld, rows);
+        } else {
+          const int ncols = (part == 3 || part == 6) ? 1 : N;
+          Soa<float> hi, lw;
+          int stride; /* element index of (row r, column cc): cc * stride + r */
+          switch (part) {
+            case 1: hi = a.ce.H, lw = lo.H, stride = N; break;
+            case 2: hi = a.ce.F, lw = lo.F, stride = N; break;
+            case 3: hi = a.ce.c, lw = lo.c, stride = 0; break;
+            case 5: hi = a.ce.G, lw = lo.G, stride = MX; break;
+            default: hi = a.ce.o, lw = lo.o, stride = 0; break;
+          }
+          const bool negate = part == 2;
+          for (int cc = 0; cc < ncols; ++cc) {
+            df col[MX];
+#pragma unroll
+            for (int r = 0; r < MX; ++r) {
+              col[r] = r < rows ? split(mine[cc * ld + r]) : make(0.0f);
+              if (negate) col[r] = neg(col[r]);
+            }
+            V.apply(col);
+#pragma unroll
+            for (int r = 0; r < MX; ++r) {
+              if (r >= rows) continue;
+              hi.at(cc * stride + r, q) = col[r].hi;
+              lw.at(cc * stride + r, q) = col[r].lo;
+            }
           }
         }
       }
@@ -963,7 +1183,7 @@ __global__ void tail_kernel(Args<T, TI> a)
     auto Di = [&](int i) -> T { return dv[i]; };
     auto xv = [&](int i) -> T& { return W[n * ld + i]; };
     solve_upper(Ru, Di, n, xv);
-    for (int i = 0; i < n; ++i) x[i] = (double)W[n * ld + i];
+    for (int i = 0; i < n; ++i) x[i] = ukg_df::widen(W[n * ld + i]);
     if (S) {
       for (int q = 0; q < n; ++q) {
         for (int i = 0; i < n; ++i) Ri[q * n + i] = (i == q) ? T(1) : T(0);
@@ -974,7 +1194,7 @@ __global__ void tail_kernel(Args<T, TI> a)
         for (int i = 0; i < n; ++i) {
           T s = T(0);
           for (int k = (i > j ? i : j); k < n; ++k) s = fma(Ri[k * n + i], Ri[k * n + j], s);
-          S[(int64_t)j * n + i] = (double)s;
+          S[(int64_t)j * n + i] = ukg_df::widen(s);
         }
     }
     if (bad) atomicOr(a.flag, 2);
@@ -1081,21 +1301,21 @@ __global__ void __launch_bounds__(BS ? BS : 1024) solve_kernel(Args<T, T> a, int
   if (hp) {
     const double* xm = a.state + om * n;
     for (int k = 0; k < n; ++k) {
-      const T xk = (T)xm[k];
+      const T xk = ukg_df::narrow<T>(xm[k]);
       for (int i = 0; i < n; ++i) pv[i] = fma(-Fs[k * n + i], xk, pv[i]);
     }
   }
   if (hn) {
     const double* xp = a.state + op * n;
     for (int k = 0; k < n; ++k) {
-      const T xk = (T)xp[k];
+      const T xk = ukg_df::narrow<T>(xp[k]);
       for (int i = 0; i < n; ++i) pv[i] = fma(-Ys[k * n + i], xk, pv[i]);
     }
   }
   auto pvr = [&](int i) -> T& { return pv[i]; };
   solve_upper(Ru, Di, n, pvr);
   double* xo = a.state + oj * n;
-  for (int i = 0; i < n; ++i) xo[i] = (double)pv[i];
+  for (int i = 0; i < n; ++i) xo[i] = ukg_df::widen(pv[i]);
   if (!want_cov) {
     if (bad) atomicOr(a.flag, 2);
     return;
@@ -1109,12 +1329,12 @@ __global__ void __launch_bounds__(BS ? BS : 1024) solve_kernel(Args<T, T> a, int
   for (int q = q0; q < q1; ++q) {
     /* column q of Sigma */
     if (q < n) {
-      for (int i = 0; i < n; ++i) sg[i] = (T)Smm[(int64_t)q * n + i];
+      for (int i = 0; i < n; ++i) sg[i] = ukg_df::narrow<T>(Smm[(int64_t)q * n + i]);
       for (int i = 0; i < n; ++i) sg[n + i] = hn ? a.nr.U.at(i * n + q, smp) : T(0); /* Smp[q, :] */
     } else {
       const int qq = q - n;
       for (int i = 0; i < n; ++i) sg[i] = hp ? a.nr.U.at(qq * n + i, smp) : T(0);
-      for (int i = 0; i < n; ++i) sg[n + i] = (T)Spp[(int64_t)qq * n + i];
+      for (int i = 0; i < n; ++i) sg[n + i] = ukg_df::narrow<T>(Spp[(int64_t)qq * n + i]);
     }
     /* pv = B sigma */
     for (int i = 0; i < n; ++i) pv[i] = T(0);
@@ -1163,7 +1383,7 @@ __global__ void __launch_bounds__(BS ? BS : 1024) solve_kernel(Args<T, T> a, int
   }
   double* So = a.cov + oj * nn;
   for (int c = 0; c < n; ++c)
-    for (int i = 0; i < n; ++i) So[(int64_t)c * n + i] = (double)M[i * n + c];
+    for (int i = 0; i < n; ++i) So[(int64_t)c * n + i] = ukg_df::widen(M[i * n + c]);
   if (bad) atomicOr(a.flag, 2);
 }
 
@@ -1280,7 +1500,107 @@ __global__ void atr_kernel(Args<float, float> a, RawDev raw, Soa<double> wE, Soa
     double s = zp.at(c, q);
     if (i + 1 < k)
       for (int p = 0; p < n; ++p) s = fma(-F1[c * n + p], wE.at(p, q + 1), s);
-    z0.at(c, q) = (float)s;
+    z0.at(c, q) = ukg_df::f64_to_f32(s);
+  }
+}
+
+/* The same right-hand side z, for the double-float weighed equations that
+ * weigh_df_kernel leaves at level 0 (FP32 high parts in the level-0 arrays,
+ * low parts in `lo`): with the weighed evolution H~ x_i + F~ x_{i-1} = c~ and
+ * observation G~ x_i = o~ (F~ = -V F),
+ *   r~_i = c~_i - H~_i x_i - F~_i x_{i-1},   s~_i = o~_i - G~_i x_i,
+ *   z_i  = H~_i^T r~_i + G~_i^T s~_i + F~_{i+1}^T r~_{i+1}
+ * in df arithmetic on the FP32 pipe.  Block b handles steps g0 = b(B-1) ..
+ * g0+B-1: every thread forms u = F~^T r~ for its step, the first B-1 also z,
+ * and thread k adds thread k+1's u, so the next step's term needs no second
+ * pass.  The level-0 arrays are element-major, so every load is coalesced.
+ * Writes z rounded to FP32.                                                  */
+template <int N, int MX, int B>
+__global__ void __launch_bounds__(B, 4) residual_df_kernel(Args<float, float> a, Eq<float> lo, Soa<float> z0,
+                                                        int64_t nsteps)
+{
+  using namespace ukg_df;
+  __shared__ float ush[2 * N][B];
+  const int tid = threadIdx.x;
+  const int64_t g = (int64_t)blockIdx.x * (B - 1) + tid;
+  const bool live = g < nsteps, own = tid < B - 1;
+  const Eq<float>& E = a.ce;
+  df z[N], u[N];
+#pragma unroll
+  for (int c = 0; c < N; ++c) z[c] = u[c] = make(0.0f);
+  int64_t q = 0;
+  bool has_next = false;
+  if (live) {
+    const int t = find_track(a.track_start, a.ntracks, g);
+    const int64_t i = g - a.track_start[t];
+    has_next = g + 1 < a.track_start[t + 1];
+    q = a.ct.slot[t] + i;
+    auto ld = [&](const Soa<float>& h, const Soa<float>& l, int e) { return df{h.at(e, q), l.at(e, q)}; };
+    const double* xg = a.state + g * N;
+    df xn[N]; /* -x_i */
+#pragma unroll
+    for (int c = 0; c < N; ++c) xn[c] = neg(split(xg[c]));
+    if (i > 0) {
+      df r[N];
+#pragma unroll
+      for (int p = 0; p < N; ++p) r[p] = ld(E.c, lo.c, p);
+#pragma unroll
+      for (int c = 0; c < N; ++c) {
+        const df xm = neg(split(xg[c - N]));
+#pragma unroll
+        for (int p = 0; p < N; ++p) {
+          r[p] = ukg_df::fma(ld(E.H, lo.H, c * N + p), xn[c], r[p]);
+          r[p] = ukg_df::fma(ld(E.F, lo.F, c * N + p), xm, r[p]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < N; ++c) {
+        df su = u[c], sz = z[c];
+#pragma unroll
+        for (int p = 0; p < N; ++p) {
+          su = ukg_df::fma(ld(E.F, lo.F, c * N + p), r[p], su);
+          if (own) sz = ukg_df::fma(ld(E.H, lo.H, c * N + p), r[p], sz);
+        }
+        u[c] = su;
+        z[c] = sz;
+      }
+    }
+    const int m = E.m[q];
+    if (own && m > 0) {
+      df s[MX];
+#pragma unroll
+      for (int p = 0; p < MX; ++p) {
+        s[p] = make(0.0f);
+        if (p < m) {
+          df sp = ld(E.o, lo.o, p);
+#pragma unroll
+          for (int c = 0; c < N; ++c) sp = ukg_df::fma(ld(E.G, lo.G, c * MX + p), xn[c], sp);
+          s[p] = sp;
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < N; ++c) {
+        df sz = z[c];
+#pragma unroll
+        for (int p = 0; p < MX; ++p)
+          if (p < m) sz = ukg_df::fma(ld(E.G, lo.G, c * MX + p), s[p], sz);
+        z[c] = sz;
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    ush[2 * c][tid] = u[c].hi;
+    ush[2 * c + 1][tid] = u[c].lo;
+  }
+  __syncthreads();
+  if (live && own) {
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      df zc = z[c];
+      if (has_next) zc = add(zc, df{ush[2 * c][tid + 1], ush[2 * c + 1][tid + 1]});
+      z0.at(c, q) = round_df(zc);
+    }
   }
 }
 
@@ -1338,7 +1658,7 @@ __global__ void rt_base_kernel(Args<float, float> a, Soa<float> zc, Soa<float> t
   solve_upper_t(Ru, Di, n, v);
   solve_upper(Ru, Di, n, v);
   double* d = a.state + orig_step(a.track_start, a.level, t, 0) * n;
-  for (int i = 0; i < n; ++i) d[i] = (double)tmp.at(i, item);
+  for (int i = 0; i < n; ++i) d[i] = ukg_df::widen(tmp.at(i, item));
 }
 
 __global__ void add_kernel(double* x, const double* d, int64_t count)
@@ -1351,6 +1671,21 @@ __global__ void add_kernel(double* x, const double* d, int64_t count)
  * host side: plan, workspace, launches
  * ------------------------------------------------------------------------ */
 constexpr int kMaxLevels = 64;
+constexpr int kResidBS = 128;
+
+/* double-float weighing and residual kernels for (n, mx), or null (FP32
+ * weighing and the FP64 residual) */
+struct DfKernels {
+  void (*weigh)(Args<float, float>, Eq<float>, RawDev, int64_t, int) = nullptr;
+  void (*resid)(Args<float, float>, Eq<float>, Soa<float>, int64_t) = nullptr;
+};
+DfKernels df_kernels(int n, int mx)
+{
+  DfKernels k;
+  if (n == 6 && mx == 6) k.weigh = weigh_df_kernel<6, 6>, k.resid = residual_df_kernel<6, 6, kResidBS>;
+  if (n == 4 && mx == 4) k.weigh = weigh_df_kernel<4, 4>, k.resid = residual_df_kernel<4, 4, kResidBS>;
+  return k;
+}
 
 struct LevelPlan {
   int64_t S = 0, E = 0, npairs = 0, nsolve = 0, ntail = 0;
@@ -1370,6 +1705,7 @@ struct Plan {
   size_t o_eqB = 0, o_mB = 0;      /* even levels >= 2 in FP32 mode          */
   size_t o_rec[kMaxLevels] = {0}, o_U[kMaxLevels] = {0};
   size_t o_z[kMaxLevels] = {0}, o_y[kMaxLevels] = {0}, o_baseR = 0, o_dx = 0, o_tmp = 0, o_rE = 0, o_rO = 0;
+  size_t o_eq0lo = 0; /* low parts of the double-float level-0 equations */
   size_t bytes = 0;
   int64_t S0 = 0, S1 = 0, S2 = 0;
 };
@@ -1456,8 +1792,12 @@ size_t build_plan(const kalman_gpu_problem_t* p, bool want_cov, bool fp32, bool 
     P.o_baseR = take((size_t)std::max(T, 1) * nn * sizeof(float));
     P.o_tmp = take((size_t)std::max(T, 1) * n * sizeof(float));
     P.o_dx = take((size_t)std::max<int64_t>(p->nsteps, 1) * n * sizeof(double));
-    P.o_rE = take((size_t)P.S0 * n * sizeof(double));
-    P.o_rO = take((size_t)P.S0 * n * sizeof(double));
+    if (df_kernels(n, mx).resid) { /* low parts of the double-float level-0 equations */
+      P.o_eq0lo = take((size_t)P.S0 * eqd * sizeof(float));
+    } else { /* the FP64 residual's intermediate arrays */
+      P.o_rE = take((size_t)P.S0 * n * sizeof(double));
+      P.o_rO = take((size_t)P.S0 * n * sizeof(double));
+    }
   }
   P.bytes = bytes;
   return pos;
@@ -1629,6 +1969,15 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
   const int kSolve = P.fp32 ? UKG_K_SOLVE32 : UKG_K_SOLVE;
   Soa<T> baseR{P.refine ? (T*)(B + P.o_baseR) : nullptr, std::max(T_, 1)};
 
+  /* double-float level-0 weighing and refinement residual where compiled */
+  DfKernels DK;
+  if constexpr (sizeof(T) == sizeof(float)) DK = df_kernels(n, mx);
+  const bool use_df = DK.resid != nullptr && P.refine && P.o_eq0lo != 0;
+  if (!use_df) DK = DfKernels();
+  Eq<float> eq0lo;
+  memset(&eq0lo, 0, sizeof(eq0lo));
+  if (use_df) eq0lo = eq_at<float>(B, P.o_eq0lo, P.o_m0, P.S0, n, mx);
+
   /* ---- level 0: weighing ---- */
   const RawDev raw{p->H, p->F, p->c, p->K, p->G, p->o, p->C, p->K_type, p->C_type, p->obs_rows, p->mmax};
   {
@@ -1641,7 +1990,19 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
     w.ntracks = T_;
     w.track_start = dtab + P.off_ts;
     w.flag = dflag;
-    if (staged)
+    bool done = false;
+    if constexpr (sizeof(T) == sizeof(float)) {
+      const size_t smem_df = 16 + (size_t)kWeighBS * blk * sizeof(double);
+      if (DK.weigh && smem_df <= (size_t)optin) {
+        cudaFuncSetAttribute(DK.weigh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_df);
+        UKG_LAUNCH(UKG_K_WEIGH, st,
+                   (DK.weigh<<<grid(p->nsteps, kWeighBS), kWeighBS, smem_df, st>>>(w, eq0lo, raw, p->nsteps,
+                                                                                    (align_bits & 15) == 0)));
+        done = true;
+      }
+    }
+    if (done) {
+    } else if (staged)
       UKG_LAUNCH(UKG_K_WEIGH, st,
                  (weigh_staged_kernel<T><<<grid(p->nsteps, kWeighBS), kWeighBS, weigh_smem, st>>>(w, raw, p->nsteps,
                                                                                                    blk)));
@@ -1695,12 +2056,17 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
         memset(&r, 0, sizeof(r));
         common(r, 0);
         r.ce = eq0();
-        Soa<double> wE{(double*)(B + P.o_rE), P.S0}, zp{(double*)(B + P.o_rO), P.S0};
         Soa<float> z0{(float*)(B + P.o_z[0]), std::max<int64_t>(lp[0].S, 1)};
-        UKG_LAUNCH(UKG_K_RESID, st,
-                   (residual_kernel<<<grid(p->nsteps, br), br, br * pt_res, st>>>(r, raw, wE, zp, p->nsteps)));
-        UKG_LAUNCH(UKG_K_RESID, st,
-                   (atr_kernel<<<grid(p->nsteps, 128), 128, 0, st>>>(r, raw, wE, zp, z0, p->nsteps)));
+        if (DK.resid) {
+          UKG_LAUNCH(UKG_K_RESID, st,
+                     (DK.resid<<<grid(p->nsteps, kResidBS - 1), kResidBS, 0, st>>>(r, eq0lo, z0, p->nsteps)));
+        } else {
+          Soa<double> wE{(double*)(B + P.o_rE), P.S0}, zp{(double*)(B + P.o_rO), P.S0};
+          UKG_LAUNCH(UKG_K_RESID, st,
+                     (residual_kernel<<<grid(p->nsteps, br), br, br * pt_res, st>>>(r, raw, wE, zp, p->nsteps)));
+          UKG_LAUNCH(UKG_K_RESID, st,
+                     (atr_kernel<<<grid(p->nsteps, 128), 128, 0, st>>>(r, raw, wE, zp, z0, p->nsteps)));
+        }
       }
       for (int l = 0; l < nlev; ++l) {
         Args<float, float> a;
