@@ -1661,6 +1661,149 @@ __global__ void rt_base_kernel(Args<float, float> a, Soa<float> zc, Soa<float> t
   for (int i = 0; i < n; ++i) d[i] = ukg_df::widen(tmp.at(i, item));
 }
 
+/* ---------------------------------------------------------------------------
+ * FP32 state-only back-substitution and refinement transpose solves with the
+ * blocks in registers (compile-time n): every load of a thread is issued
+ * before its arithmetic, which keeps many loads in flight per SM.  Same
+ * arithmetic as solve_kernel (want_cov = 0), rt_even_kernel and rt_odd_kernel.
+ * ------------------------------------------------------------------------ */
+template <int N>
+__global__ void __launch_bounds__(128) solve_state_reg_kernel(Args<float, float> a)
+{
+  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= a.ct.nsolve) return;
+  const int t = find_track(a.ct.solve, a.ntracks, item);
+  const int64_t j = 2 * (item - a.ct.solve[t]), L = a.ct.L[t];
+  const bool hp = j > 0, hn = j + 1 < L;
+  const Rec<float>& Rr = a.cr;
+  float R[N][N], pv[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k)
+#pragma unroll
+    for (int i = 0; i <= k; ++i) R[k][i] = Rr.R.at(k * N + i, item);
+#pragma unroll
+  for (int i = 0; i < N; ++i) pv[i] = a.yrhs.p ? a.yrhs.at(i, item) : Rr.rhs.at(i, item);
+  if (hp) {
+    const double* xm = a.state + orig_step(a.track_start, a.level, t, j - 1) * N;
+    float F[N][N], x[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      x[k] = ukg_df::f64_to_f32(xm[k]);
+#pragma unroll
+      for (int i = 0; i < N; ++i) F[k][i] = Rr.Ft.at(k * N + i, item);
+    }
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+#pragma unroll
+      for (int i = 0; i < N; ++i) pv[i] = fmaf(-F[k][i], x[k], pv[i]);
+  }
+  if (hn) {
+    const double* xp = a.state + orig_step(a.track_start, a.level, t, j + 1) * N;
+    float Y[N][N], x[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      x[k] = ukg_df::f64_to_f32(xp[k]);
+#pragma unroll
+      for (int i = 0; i < N; ++i) Y[k][i] = Rr.Y.at(k * N + i, item);
+    }
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+#pragma unroll
+      for (int i = 0; i < N; ++i) pv[i] = fmaf(-Y[k][i], x[k], pv[i]);
+  }
+  bool bad = false;
+#pragma unroll
+  for (int i = N - 1; i >= 0; --i) {
+    float sm = pv[i];
+#pragma unroll
+    for (int k = i + 1; k < N; ++k) sm = fmaf(-R[k][i], pv[k], sm);
+    bad |= R[i][i] == 0.0f;
+    pv[i] = sm * (1.0f / R[i][i]);
+  }
+  double* xo = a.state + orig_step(a.track_start, a.level, t, j) * N;
+#pragma unroll
+  for (int i = 0; i < N; ++i) xo[i] = ukg_df::f32_to_f64(pv[i]);
+  if (bad) atomicOr(a.flag, 2);
+}
+
+template <int N>
+__global__ void __launch_bounds__(128) rt_even_reg_kernel(Args<float, float> a, Soa<float> zc, Soa<float> yc)
+{
+  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= a.ct.nsolve) return;
+  const int t = find_track(a.ct.solve, a.ntracks, item);
+  const int64_t sz = a.ct.slot[t] + 2 * (item - a.ct.solve[t]);
+  float R[N][N], y[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    y[k] = zc.at(k, sz);
+#pragma unroll
+    for (int i = 0; i <= k; ++i) R[k][i] = a.cr.R.at(k * N + i, item);
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    float sm = y[i];
+#pragma unroll
+    for (int k = 0; k < i; ++k) sm = fmaf(-R[i][k], y[k], sm);
+    y[i] = sm * (1.0f / R[i][i]);
+    yc.at(i, item) = y[i];
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(128) rt_odd_reg_kernel(Args<float, float> a, Soa<float> zc, Soa<float> yc,
+                                                         Soa<float> zn)
+{
+  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= a.ct.npairs) return;
+  const int t = find_track(a.ct.pair, a.ntracks, item);
+  const int64_t p = item - a.ct.pair[t], L = a.ct.L[t];
+  const int64_t so = a.ct.slot[t] + 2 * p + 1, sn = a.nt.slot[t] + p;
+  const int64_t e0 = a.ct.solve[t] + p, e1 = e0 + 1;
+  const bool right = 2 * p + 2 <= L - 1;
+  float Y[N][N], y0[N], z[N];
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    z[c] = zc.at(c, so);
+    y0[c] = yc.at(c, e0);
+#pragma unroll
+    for (int r = 0; r < N; ++r) Y[c][r] = a.cr.Y.at(c * N + r, e0);
+  }
+  if (right) {
+    float F[N][N], y1[N];
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      y1[c] = yc.at(c, e1);
+#pragma unroll
+      for (int r = 0; r < N; ++r) F[c][r] = a.cr.Ft.at(c * N + r, e1);
+    }
+#pragma unroll
+    for (int c = 0; c < N; ++c)
+#pragma unroll
+      for (int r = 0; r < N; ++r) z[c] = fmaf(-F[c][r], y1[r], z[c]);
+  }
+#pragma unroll
+  for (int c = 0; c < N; ++c) {
+    float sm = z[c];
+#pragma unroll
+    for (int r = 0; r < N; ++r) sm = fmaf(-Y[c][r], y0[r], sm);
+    zn.at(c, sn) = sm;
+  }
+}
+
+struct RegSolves {
+  void (*solve)(Args<float, float>) = nullptr;
+  void (*rt_even)(Args<float, float>, Soa<float>, Soa<float>) = nullptr;
+  void (*rt_odd)(Args<float, float>, Soa<float>, Soa<float>, Soa<float>) = nullptr;
+};
+RegSolves reg_solves(int n)
+{
+  RegSolves r;
+  if (n == 6) r.solve = solve_state_reg_kernel<6>, r.rt_even = rt_even_reg_kernel<6>, r.rt_odd = rt_odd_reg_kernel<6>;
+  if (n == 4) r.solve = solve_state_reg_kernel<4>, r.rt_even = rt_even_reg_kernel<4>, r.rt_odd = rt_odd_reg_kernel<4>;
+  return r;
+}
+
 __global__ void add_kernel(double* x, const double* d, int64_t count)
 {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1976,6 +2119,8 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
   if (!use_df) DK = DfKernels();
   Eq<float> eq0lo;
   memset(&eq0lo, 0, sizeof(eq0lo));
+  RegSolves RS; /* register-resident FP32 solves where compiled */
+  if constexpr (sizeof(T) == sizeof(float)) RS = reg_solves(n);
   if (use_df) eq0lo = eq_at<float>(B, P.o_eq0lo, P.o_m0, P.S0, n, mx);
 
   /* ---- level 0: weighing ---- */
@@ -2042,8 +2187,14 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
     Args<T, T> a;
     memset(&a, 0, sizeof(a));
     common(a, l);
-    if (lp[l].nsolve > 0)
-      UKG_LAUNCH(kSolve, st, (K.solve<<<grid(lp[l].nsolve, bs), bs, bs * pt_solve, st>>>(a, want_cov ? 1 : 0)));
+    if (lp[l].nsolve == 0) continue;
+    if constexpr (sizeof(T) == sizeof(float)) {
+      if (RS.solve && !want_cov) {
+        UKG_LAUNCH(kSolve, st, (RS.solve<<<grid(lp[l].nsolve, 128), 128, 0, st>>>(a)));
+        continue;
+      }
+    }
+    UKG_LAUNCH(kSolve, st, (K.solve<<<grid(lp[l].nsolve, bs), bs, bs * pt_solve, st>>>(a, want_cov ? 1 : 0)));
   }
   /* ---- refinement sweeps (FP32 factors only) ---- */
   if constexpr (sizeof(T) == sizeof(float)) {
@@ -2076,11 +2227,18 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
         a.cov = nullptr;
         Soa<float> zc{(float*)(B + P.o_z[l]), std::max<int64_t>(lp[l].S, 1)};
         Soa<float> yc{(float*)(B + P.o_y[l]), std::max<int64_t>(lp[l].E, 1)};
-        if (lp[l].nsolve > 0)
-          UKG_LAUNCH(UKG_K_RT, st, (rt_even_kernel<<<grid(lp[l].nsolve, 128), 128, 0, st>>>(a, zc, yc)));
+        if (lp[l].nsolve > 0) {
+          if (RS.rt_even)
+            UKG_LAUNCH(UKG_K_RT, st, (RS.rt_even<<<grid(lp[l].nsolve, 128), 128, 0, st>>>(a, zc, yc)));
+          else
+            UKG_LAUNCH(UKG_K_RT, st, (rt_even_kernel<<<grid(lp[l].nsolve, 128), 128, 0, st>>>(a, zc, yc)));
+        }
         if (lp[l].npairs > 0 && l + 1 < nlev) {
           Soa<float> zn{(float*)(B + P.o_z[l + 1]), std::max<int64_t>(lp[l + 1].S, 1)};
-          UKG_LAUNCH(UKG_K_RT, st, (rt_odd_kernel<<<grid(lp[l].npairs, 128), 128, 0, st>>>(a, zc, yc, zn)));
+          if (RS.rt_odd)
+            UKG_LAUNCH(UKG_K_RT, st, (RS.rt_odd<<<grid(lp[l].npairs, 128), 128, 0, st>>>(a, zc, yc, zn)));
+          else
+            UKG_LAUNCH(UKG_K_RT, st, (rt_odd_kernel<<<grid(lp[l].npairs, 128), 128, 0, st>>>(a, zc, yc, zn)));
         }
         if (lp[l].ntail > 0) {
           Soa<float> tmp{(float*)(B + P.o_tmp), std::max(T_, 1)};
@@ -2094,7 +2252,10 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
         a.state = dx;
         a.cov = nullptr;
         a.yrhs = Soa<float>{(float*)(B + P.o_y[l]), std::max<int64_t>(lp[l].E, 1)};
-        if (lp[l].nsolve > 0)
+        if (lp[l].nsolve == 0) continue;
+        if (RS.solve)
+          UKG_LAUNCH(UKG_K_RSOLVE, st, (RS.solve<<<grid(lp[l].nsolve, 128), 128, 0, st>>>(a)));
+        else
           UKG_LAUNCH(UKG_K_RSOLVE, st, (K.solve<<<grid(lp[l].nsolve, bs), bs, bs * pt_solve, st>>>(a, 0)));
       }
       const int64_t cnt = p->nsteps * n;
