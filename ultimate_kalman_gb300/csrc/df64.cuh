@@ -129,6 +129,26 @@ __device__ __forceinline__ df fma(df a, df b, df acc)
   return fast_two_sum(s.hi, s.lo + (acc.lo + e));
 }
 
+/* Unnormalized accumulator for a sum of products (the compensated dot
+ * product "Dot2" of Ogita, Rump and Oishi, 2005, with double-float operands):
+ * hi is the running FP32 sum, made exact by TwoSum, and lo collects its
+ * rounding errors and the products' low parts; finish() normalizes once.    */
+struct acc {
+  float hi, lo;
+};
+__device__ __forceinline__ acc start(df a) { return acc{a.hi, a.lo}; }
+__device__ __forceinline__ void add_prod(acc& s, df a, df b)
+{
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  const df t = two_sum(s.hi, p);
+  s.hi = t.hi;
+  s.lo = __fadd_rn(s.lo, __fadd_rn(t.lo, e));
+}
+__device__ __forceinline__ df finish(acc s) { return two_sum(s.hi, s.lo); }
+
 /* 1 / d by one Newton step on the FP32 reciprocal: r0 (1 + (1 - d r0)) */
 __device__ __forceinline__ df rcp(df d)
 {

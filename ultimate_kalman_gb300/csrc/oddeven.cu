@@ -614,9 +614,10 @@ struct DfWeights {
 #pragma unroll
       for (int j = 0; j < R; ++j) {
         if (j >= rows) continue;
-        df d = v[j * R + j];
+        acc da = start(v[j * R + j]);
 #pragma unroll
-        for (int k = 0; k < j; ++k) d = ukg_df::fma(neg(v[k * R + j]), v[k * R + j], d);
+        for (int k = 0; k < j; ++k) add_prod(da, neg(v[k * R + j]), v[k * R + j]);
+        df d = finish(da);
         if (!(d.hi > 0.0f)) {
           ok = false;
           d = make(1.0f);
@@ -626,10 +627,10 @@ struct DfWeights {
 #pragma unroll
         for (int i = j + 1; i < R; ++i) {
           if (i >= rows) continue;
-          df sm = v[j * R + i];
+          acc sm = start(v[j * R + i]);
 #pragma unroll
-          for (int k = 0; k < j; ++k) sm = ukg_df::fma(neg(v[k * R + i]), v[k * R + j], sm);
-          v[j * R + i] = mul(sm, r);
+          for (int k = 0; k < j; ++k) add_prod(sm, neg(v[k * R + i]), v[k * R + j]);
+          v[j * R + i] = mul(finish(sm), r);
         }
       }
     }
@@ -643,11 +644,10 @@ struct DfWeights {
       df t[R];
 #pragma unroll
       for (int i = j + 1; i < R; ++i) {
-        df sm = make(0.0f);
+        acc sm = start(make(0.0f));
 #pragma unroll
-        for (int k = j + 1; k <= i; ++k)
-          if (i < rows) sm = ukg_df::fma(v[k * R + i], v[j * R + k], sm);
-        t[i] = mul(sm, najj);
+        for (int k = j + 1; k <= i; ++k) add_prod(sm, v[k * R + i], v[j * R + k]);
+        t[i] = mul(finish(sm), najj);
       }
 #pragma unroll
       for (int i = j + 1; i < R; ++i)
@@ -657,25 +657,21 @@ struct DfWeights {
     return ok;
   }
 
-  /* col <- V col on the first `rows` entries */
+  /* col <- V col on the first `rows` entries (V is zero past `rows`, so the
+   * sums need no guards) */
   __device__ __forceinline__ void apply(ukg_df::df (&col)[R]) const
   {
     using namespace ukg_df;
     df t[R];
 #pragma unroll
     for (int i = R - 1; i >= 0; --i) {
-      df sm = make(0.0f);
+      acc sm = start(make(0.0f));
 #pragma unroll
-      for (int j = 0; j <= i; ++j)
-        if (i < rows) sm = ukg_df::fma(v[j * R + i], col[j], sm);
-      t[i] = sm;
-    }
-    if (full) {
+      for (int j = 0; j <= i; ++j) add_prod(sm, v[j * R + i], col[j]);
+      if (full)
 #pragma unroll
-      for (int i = 0; i < R; ++i)
-#pragma unroll
-        for (int j = i + 1; j < R; ++j)
-          if (j < rows) t[i] = ukg_df::fma(v[j * R + i], col[j], t[i]);
+        for (int j = i + 1; j < R; ++j) add_prod(sm, v[j * R + i], col[j]);
+      t[i] = finish(sm);
     }
 #pragma unroll
     for (int i = 0; i < R; ++i) col[i] = t[i];
@@ -1515,11 +1511,12 @@ __global__ void atr_kernel(Args<float, float> a, RawDev raw, Soa<double> wE, Soa
  * and thread k adds thread k+1's u, so the next step's term needs no second
  * pass.  The level-0 arrays are element-major, so every load is coalesced.
  * Writes z rounded to FP32.                                                  */
-template <int N, int MX, int B>
+template <int N, int MM, int B>
 __global__ void __launch_bounds__(B, 4) residual_df_kernel(Args<float, float> a, Eq<float> lo, Soa<float> z0,
-                                                        int64_t nsteps)
+                                                           int64_t nsteps)
 {
   using namespace ukg_df;
+  constexpr int MX = MM > N ? MM : N; /* leading dimension of the level-0 G */
   __shared__ float ush[2 * N][B];
   const int tid = threadIdx.x;
   const int64_t g = (int64_t)blockIdx.x * (B - 1) + tid;
@@ -1541,50 +1538,52 @@ __global__ void __launch_bounds__(B, 4) residual_df_kernel(Args<float, float> a,
 #pragma unroll
     for (int c = 0; c < N; ++c) xn[c] = neg(split(xg[c]));
     if (i > 0) {
+      df xm[N]; /* -x_{i-1} */
+#pragma unroll
+      for (int c = 0; c < N; ++c) xm[c] = neg(split(xg[c - N]));
       df r[N];
 #pragma unroll
-      for (int p = 0; p < N; ++p) r[p] = ld(E.c, lo.c, p);
+      for (int p = 0; p < N; ++p) {
+        acc sr = start(ld(E.c, lo.c, p));
 #pragma unroll
-      for (int c = 0; c < N; ++c) {
-        const df xm = neg(split(xg[c - N]));
-#pragma unroll
-        for (int p = 0; p < N; ++p) {
-          r[p] = ukg_df::fma(ld(E.H, lo.H, c * N + p), xn[c], r[p]);
-          r[p] = ukg_df::fma(ld(E.F, lo.F, c * N + p), xm, r[p]);
+        for (int c = 0; c < N; ++c) {
+          add_prod(sr, ld(E.H, lo.H, c * N + p), xn[c]);
+          add_prod(sr, ld(E.F, lo.F, c * N + p), xm[c]);
         }
+        r[p] = finish(sr);
       }
 #pragma unroll
       for (int c = 0; c < N; ++c) {
-        df su = u[c], sz = z[c];
+        acc su = start(make(0.0f)), sz = start(make(0.0f));
 #pragma unroll
         for (int p = 0; p < N; ++p) {
-          su = ukg_df::fma(ld(E.F, lo.F, c * N + p), r[p], su);
-          if (own) sz = ukg_df::fma(ld(E.H, lo.H, c * N + p), r[p], sz);
+          add_prod(su, ld(E.F, lo.F, c * N + p), r[p]);
+          if (own) add_prod(sz, ld(E.H, lo.H, c * N + p), r[p]);
         }
-        u[c] = su;
-        z[c] = sz;
+        u[c] = finish(su);
+        z[c] = finish(sz);
       }
     }
     const int m = E.m[q];
     if (own && m > 0) {
-      df s[MX];
+      df s[MM];
 #pragma unroll
-      for (int p = 0; p < MX; ++p) {
+      for (int p = 0; p < MM; ++p) {
         s[p] = make(0.0f);
         if (p < m) {
-          df sp = ld(E.o, lo.o, p);
+          acc sp = start(ld(E.o, lo.o, p));
 #pragma unroll
-          for (int c = 0; c < N; ++c) sp = ukg_df::fma(ld(E.G, lo.G, c * MX + p), xn[c], sp);
-          s[p] = sp;
+          for (int c = 0; c < N; ++c) add_prod(sp, ld(E.G, lo.G, c * MX + p), xn[c]);
+          s[p] = finish(sp);
         }
       }
 #pragma unroll
       for (int c = 0; c < N; ++c) {
-        df sz = z[c];
+        acc sz = start(z[c]);
 #pragma unroll
-        for (int p = 0; p < MX; ++p)
-          if (p < m) sz = ukg_df::fma(ld(E.G, lo.G, c * MX + p), s[p], sz);
-        z[c] = sz;
+        for (int p = 0; p < MM; ++p)
+          if (p < m) add_prod(sz, ld(E.G, lo.G, c * MX + p), s[p]);
+        z[c] = finish(sz);
       }
     }
   }
@@ -1822,11 +1821,17 @@ struct DfKernels {
   void (*weigh)(Args<float, float>, Eq<float>, RawDev, int64_t, int) = nullptr;
   void (*resid)(Args<float, float>, Eq<float>, Soa<float>, int64_t) = nullptr;
 };
-DfKernels df_kernels(int n, int mx)
+DfKernels df_kernels(int n, int mmax)
 {
   DfKernels k;
-  if (n == 6 && mx == 6) k.weigh = weigh_df_kernel<6, 6>, k.resid = residual_df_kernel<6, 6, kResidBS>;
-  if (n == 4 && mx == 4) k.weigh = weigh_df_kernel<4, 4>, k.resid = residual_df_kernel<4, 4, kResidBS>;
+  const int mx = mmax > n ? mmax : n;
+  if (n == 6 && mx == 6) k.weigh = weigh_df_kernel<6, 6>;
+  if (n == 4 && mx == 4) k.weigh = weigh_df_kernel<4, 4>;
+#define UKG_DF(N_, M_)                                                                                              \
+  if (n == N_ && mmax == M_) k.resid = residual_df_kernel<N_, M_, kResidBS>;
+  UKG_DF(6, 6) UKG_DF(6, 3) UKG_DF(6, 2) UKG_DF(4, 4) UKG_DF(4, 2)
+#undef UKG_DF
+  if (!k.weigh || !k.resid) k = DfKernels(); /* both or neither */
   return k;
 }
 
@@ -1935,7 +1940,7 @@ size_t build_plan(const kalman_gpu_problem_t* p, bool want_cov, bool fp32, bool 
     P.o_baseR = take((size_t)std::max(T, 1) * nn * sizeof(float));
     P.o_tmp = take((size_t)std::max(T, 1) * n * sizeof(float));
     P.o_dx = take((size_t)std::max<int64_t>(p->nsteps, 1) * n * sizeof(double));
-    if (df_kernels(n, mx).resid) { /* low parts of the double-float level-0 equations */
+    if (df_kernels(n, p->mmax).resid) { /* low parts of the double-float level-0 equations */
       P.o_eq0lo = take((size_t)P.S0 * eqd * sizeof(float));
     } else { /* the FP64 residual's intermediate arrays */
       P.o_rE = take((size_t)P.S0 * n * sizeof(double));
@@ -2114,7 +2119,7 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
 
   /* double-float level-0 weighing and refinement residual where compiled */
   DfKernels DK;
-  if constexpr (sizeof(T) == sizeof(float)) DK = df_kernels(n, mx);
+  if constexpr (sizeof(T) == sizeof(float)) DK = df_kernels(n, p->mmax);
   const bool use_df = DK.resid != nullptr && P.refine && P.o_eq0lo != 0;
   if (!use_df) DK = DfKernels();
   Eq<float> eq0lo;
