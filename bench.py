@@ -54,7 +54,7 @@ UNIT = "steps/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--tracks", type=int, default=4096)
@@ -62,7 +62,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--sweeps", type=int, default=0, help="refinement sweeps (0: library default)")
+    ap.add_argument("--sweeps", type=int, default=1,
+                    help="refinement sweeps (one meets the 1e-9 bar with margin; 0: the library default, two)")
     return ap.parse_args()
 
 
@@ -97,7 +98,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+                                          "-lms", "50"], stdout=self.file, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
@@ -185,16 +186,20 @@ def time_smooths(D, steps, stream, **kw):
 
 
 def roofline_for(prof, fl, steps, fp64_peak, fp32_peak, hbm_peak, bytes_model):
+    """Roofline of the kernel category with the largest time.  FP64 kernels
+    are placed against the FP64 pipe or HBM, whichever fraction is higher;
+    the precision form's kernels (FP32 and double-float arithmetic on the FP32
+    pipe, far below its peak) against HBM."""
     top = max(prof, key=lambda k: prof[k][0])
     kms, kl = prof[top]
     secs = kms * 1e-3 / steps
     flops = fl.get(top, 0.0)
-    is32 = top.startswith("fp32") or top == "refine_kernel"
+    is32 = top.startswith("fp32") or top.startswith("refine") or top not in fl
     peak_f = fp32_peak if is32 else fp64_peak
     ach_f = flops / secs / 1e12
     ach_b = bytes_model.get(top, 0.0) / secs / 1e9
     frac_f, frac_b = ach_f / peak_f, ach_b / hbm_peak
-    if frac_b > frac_f:
+    if frac_b > frac_f or is32:
         r = {"bound": "hbm", "achieved": ach_b, "peak": hbm_peak, "unit": "GB/s", "frac": frac_b,
              "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
     else:
@@ -227,6 +232,7 @@ def run_gpu(args):
             torch.distributed.barrier()
 
     sampler = ClockSampler(local)
+    time.sleep(0.5)  # let the sampler start before the timed region
     stream = torch.cuda.current_stream()
     native.profile_enable(True)
     launches0 = native.launch_count()
@@ -259,10 +265,10 @@ def run_gpu(args):
     peak32 = native.measure_fp32_tflops()
     peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(REPO, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
-    fl32 = flops.plan_flops_fast_fp32(P.track_lengths(), 6, 3, sweeps=args.sweeps or 2)
+    fl32 = {}  # the precision form is placed against HBM (see roofline_for)
     fl64 = flops.plan_flops_fast(P.track_lengths(), 6, 3, covariance=True)
-    by32 = flops.plan_bytes_fast(P.track_lengths(), 6, 6, fp32=True, sweeps=args.sweeps or 2)
-    by64 = flops.plan_bytes_fast(P.track_lengths(), 6, 6, fp32=False)
+    by32 = flops.plan_bytes_fast(P.track_lengths(), 6, 3, fp32=True, sweeps=args.sweeps or 2)
+    by64 = flops.plan_bytes_fast(P.track_lengths(), 6, 3, fp32=False)
     roof = roofline_for(prof, fl32, args.steps, peak64, peak32, peaks["hbm_gbs"], by32)
     tfile = os.path.join(REPO, "profiles", "traffic_per_launch.json")
     if os.path.exists(tfile):

@@ -168,32 +168,45 @@ def plan_flops_fast_fp32(track_lengths, n, m0, sweeps=2):
             "fp32_solve_kernel": f["solve_kernel"], "refine_kernel": refine_flops(track_lengths, n, m0, sweeps)}
 
 
-def plan_bytes_fast(track_lengths, n, mx, fp32=False, sweeps=2):
-    """Algorithmic DRAM bytes per kernel class for one smoothing (states only):
-    every input block read once, every output and intermediate written once
-    and read once.  Level-0 equations are FP64; levels and records are FP32
-    in the precision form."""
+def plan_bytes_fast(track_lengths, n, m, fp32=False, sweeps=1):
+    """Algorithmic DRAM bytes per kernel category for one states-only smoothing
+    of tracks with n states and m observation rows per step: every input block
+    read once, every output and intermediate written once and read once.
+
+    Level 0 (weigh_kernel): the raw FP64 equations K, H, F, c, C, G, o in and
+    the weighed level-0 equations out -- FP64 in the plain path, FP32 high
+    plus FP32 low parts (8 bytes an entry) in the precision form.  Levels
+    l >= 1 carry g_l = min(m 2^l, n) observation rows.  The precision form's
+    levels and records are FP32 (4 bytes an entry), the plain path's FP64."""
     lengths = np.asarray(track_lengths, dtype=np.int64)
     N = float(lengths.sum())
-    eqd = 2 * n * n + n + mx * n + mx
-    raw = 3 * n * n + n + mx * n + mx + mx * mx
     t = 4.0 if fp32 else 8.0
-    out = {"weigh_kernel": N * (raw * 8 + 6 + eqd * 8 + 4)}
-    pair = solve = 0.0
+
+    def eq_rows(g):
+        return 2 * n * n + n + g * n + g
+
+    raw = (3 * n * n + n + m * n + m + m * m) * 8 + 2 + 4  # + covariance types, observation rows
+    out = {"weigh_kernel": N * (raw + eq_rows(m) * 8 + 4)}
+    rec = 3 * n * n + n
+    pair = solve = rt = 0.0
     L = lengths.copy()
     level = 0
     while (L >= 2).any():
         pairs = float(np.where(L >= 2, L // 2, 0).sum())
         evens = float(np.where(L >= 2, (L + 1) // 2, 0).sum())
-        size_in = 8.0 if level == 0 else t
-        pair += pairs * (2 * eqd * size_in + eqd * t + (3 * n * n + n) * t)
-        solve += evens * ((3 * n * n + n) * t + 3 * n * 8)
+        g, g1 = min(m << level, n), min(m << (level + 1), n)
+        pair += pairs * (2 * eq_rows(g) * t + rec * t + eq_rows(g1) * t)
+        solve += evens * ((n * (n + 1) // 2 + 2 * n * n + n) * t + 3 * n * 8)
+        rt += evens * ((n * (n + 1) // 2 + 2 * n) * 4) + pairs * ((2 * n * n + 4 * n) * 4)
         L = L // 2
         level += 1
     if fp32:
         out["fp32_pair_kernel"] = pair
         out["fp32_solve_kernel"] = solve
-        out["refine_kernel"] = sweeps * (N * (eqd * 8 + 4 * n * 8 + n * 4) + solve)
+        out["refine_residual_kernel"] = sweeps * N * (eq_rows(m) * 8 + n * 8 + n * 4)
+        out["refine_rt_kernel"] = sweeps * rt
+        out["refine_solve_kernel"] = sweeps * solve
+        out["refine_kernel"] = sweeps * N * n * 24
     else:
         out["pair_kernel"] = pair
         out["solve_kernel"] = solve
