@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fp32-only", action="store_true",
+                    help="time the precision form only (no plain FP64 pass, probes, e2e or CPU leg): profiling runs")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--sweeps", type=int, default=1,
                     help="refinement sweeps (one meets the 1e-9 bar with margin; 0: the library default, two)")
@@ -250,6 +252,14 @@ def run_gpu(args):
         ms = float(t.item())
     total_steps = P.nsteps * world
     value = total_steps / (ms * 1e-3)
+    if args.fp32_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                              "warmup": args.warmup, "ms_per_step": ms, "note": "--fp32-only profiling run",
+                              "config": config_dict(P, args.tracks, world), "gpu_launches": int(launches)}), flush=True)
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
 
     # the plain FP64 path: states + covariances, and states only
     D.smooth("oddeven", covariance=True)

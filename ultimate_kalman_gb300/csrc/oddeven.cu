@@ -31,12 +31,15 @@
  *
  * Precision.  The kernels are templates over the arithmetic type T.  FP64 is
  * the plain path.  With KALMAN_GPU_FP32_REFINE the factorization (levels,
- * records) is FP32, reading the FP64-weighed level-0 equations; the states are
- * then refined with corrected semi-normal equations: the residual r = b - A x
- * of the weighted block-bidiagonal least-squares system and z = A^T r in FP64
- * (residual_kernel), R^T y = z level by level (rt_even_kernel, rt_odd_kernel,
- * rt_base_kernel) and R d = y (solve_kernel with right-hand side y) with the
- * FP32 R factors, x += d in FP64 -- one or two sweeps.
+ * records) is FP32; the states are then refined with corrected semi-normal
+ * equations: the residual r = b - A x of the weighted block-bidiagonal
+ * least-squares system and z = A^T r in extended precision, R^T y = z level by
+ * level and R d = y with the FP32 R factors, x += d in FP64 -- one or two
+ * sweeps.  For the common shapes (n = 4, 6) the level-0 weighing and the
+ * residual run in double-float arithmetic on the FP32 pipe (weigh_df_kernel
+ * stores the weighed equations as FP32 high + low parts, residual_df_kernel
+ * reads them; df64.cuh); other shapes weigh in FP32 and form the residual in
+ * FP64 from the raw equations (residual_kernel, atr_kernel).
  *
  * Layout in HBM ("slot" = a step of a level, every track's slots start at an
  * even slot so pairs never straddle tracks):
