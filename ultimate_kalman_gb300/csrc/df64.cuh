@@ -59,17 +59,20 @@ struct df {
 
 /* Exact split of an FP64 value: hi = its leading 24 bits, lo = the next 23
  * (the last 6 bits are dropped).  Outside 2^-103 <= |x| < 2^128, lo is 0 and hi
- * the rounded FP32 value. */
+ * the rounded FP32 value.  In range, hi's exponent field is the FP64 one's low
+ * eight bits with the top bit flipped (e - 896 = e - 128 mod 256), so hi comes
+ * from one funnel shift; lo = (bits 28..6 of the low word) * 2^(e-1069) is
+ * built as 2^E0 (1 + f) - 2^E0 with E0 = e - 1046 (an exact subtraction). */
 __device__ __forceinline__ df split(double x)
 {
   const uint32_t h = (uint32_t)__double2hiint(x), l = (uint32_t)__double2loint(x);
-  const uint32_t s = h & 0x80000000u, e = (h >> 20) & 0x7ffu;
+  const uint32_t e = (h >> 20) & 0x7ffu;
   df r;
   if (e - 920u <= 230u) {
-    r.hi = __uint_as_float(s | ((e - 896u) << 23) | ((h & 0xfffffu) << 3) | (l >> 29));
-    /* lo = (bits 28..6 of l) * 2^(e-1069): build 2^E0 (1 + f) with E0 = e - 1046
-     * and subtract 2^E0 (exact) */
-    const uint32_t E = s | ((e - 919u) << 23);
+    const uint32_t t = __funnelshift_l(l, h, 3) ^ 0x40000000u;
+    const uint32_t hb = (t & 0x7fffffffu) | (h & 0x80000000u);
+    const uint32_t E = (hb & 0xff800000u) - (23u << 23);
+    r.hi = __uint_as_float(hb);
     r.lo = __uint_as_float(E | ((l >> 6) & 0x7fffffu)) - __uint_as_float(E);
   } else {
     r.hi = f64_to_f32(x);

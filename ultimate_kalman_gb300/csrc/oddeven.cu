@@ -586,37 +586,48 @@ __global__ void __launch_bounds__(kWeighBS) weigh_staged_kernel(Args<T, T> a, Ra
  * ------------------------------------------------------------------------ */
 template <int R>
 struct DfWeights {
-  ukg_df::df v[R * R]; /* the weighing V, column-major: V(i, j) at v[j * R + i] */
-  bool full;           /* 'W': every entry; otherwise V is lower triangular */
+  /* 'W': the matrix W (column-major: (i, j) at v[j * R + i]); 'C', 'U', 'F':
+   * the lower factor L below the diagonal and 1/L_jj on it; 'w' (and an
+   * unknown type, reported by the caller): the weights on the diagonal */
+  ukg_df::df v[R * R];
+  int mode; /* 0: W col, 1: diagonal, 2: L^{-1} col */
   int rows;
 
-  /* V for the covariance factor (cov: entry (i, j) at cov[j * ld + i], the
-   * first nrows rows and columns): 'W' the matrix, 'w' its diagonal, 'C'
-   * chol(cov)^{-1}, 'U'/'F' tril(cov)^{-1}.  False: not positive definite or
-   * a zero pivot.  One code path for all types keeps the kernel small.       */
+  /* the weighing for the covariance factor (cov: entry (i, j) at
+   * cov[j * ld + i], the first nrows rows and columns): 'W' col <- W col,
+   * 'w' col <- diag(cov) col, 'C' col <- chol(cov)^{-1} col, 'U'/'F'
+   * col <- tril(cov)^{-1} col.  False: not positive definite or a zero pivot. */
   __device__ __forceinline__ bool prepare(char t, const double* cov, int ld, int nrows)
   {
     using namespace ukg_df;
     rows = nrows;
-    full = t == 'W';
-    const bool diag = t == 'w', tri_in = t == 'U' || t == 'F', chol = t == 'C';
+    mode = t == 'W' ? 0 : (t == 'C' || t == 'U' || t == 'F') ? 2 : 1;
+    if (mode == 0) {
 #pragma unroll
-    for (int j = 0; j < R; ++j)
+      for (int j = 0; j < R; ++j)
 #pragma unroll
-      for (int i = 0; i < R; ++i) {
-        df e = make(i == j && !(full || diag || tri_in || chol) ? 1.0f : 0.0f);
-        if (i < rows && j < rows) {
-          if (full || ((tri_in || chol) && i >= j)) e = split(cov[j * ld + i]);
-          else if (diag && i == j) e = split(cov[i]);
-        }
-        v[j * R + i] = e;
-      }
-    if (!(tri_in || chol)) return true;
+        for (int i = 0; i < R; ++i)
+          if (i < rows && j < rows) v[j * R + i] = split(cov[j * ld + i]);
+      return true;
+    }
+    if (mode == 1) {
+#pragma unroll
+      for (int i = 0; i < R; ++i)
+        if (i < rows) v[i * R + i] = t == 'w' ? split(cov[i]) : make(1.0f);
+      return true;
+    }
     bool ok = true;
-    if (chol) { /* lower Cholesky factor in place */
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      if (j >= rows) break;
+#pragma unroll
+      for (int i = j; i < R; ++i)
+        if (i < rows) v[j * R + i] = split(cov[j * ld + i]);
+    }
+    if (t == 'C') { /* lower Cholesky factor in place, reciprocal diagonal */
 #pragma unroll
       for (int j = 0; j < R; ++j) {
-        if (j >= rows) continue;
+        if (j >= rows) break;
         acc da = start(v[j * R + j]);
 #pragma unroll
         for (int k = 0; k < j; ++k) add_prod(da, neg(v[k * R + j]), v[k * R + j]);
@@ -625,59 +636,58 @@ struct DfWeights {
           ok = false;
           d = make(1.0f);
         }
-        const df l = ukg_df::sqrt(d), r = rcp(l);
-        v[j * R + j] = l;
+        const df r = rcp(ukg_df::sqrt(d));
+        v[j * R + j] = r;
 #pragma unroll
         for (int i = j + 1; i < R; ++i) {
-          if (i >= rows) continue;
+          if (i >= rows) break;
           acc sm = start(v[j * R + i]);
 #pragma unroll
           for (int k = 0; k < j; ++k) add_prod(sm, neg(v[k * R + i]), v[k * R + j]);
           v[j * R + i] = mul(finish(sm), r);
         }
       }
-    }
-    /* L^{-1} in place, last column first: column j of the inverse is
-     * -(1/L_jj) Linv[j+1:, j+1:] L[j+1:, j] below the diagonal 1/L_jj */
+    } else {
 #pragma unroll
-    for (int j = R - 1; j >= 0; --j) {
-      if (j >= rows) continue;
-      ok &= v[j * R + j].hi != 0.0f;
-      const df ajj = rcp(v[j * R + j]), najj = neg(ajj);
-      df t[R];
-#pragma unroll
-      for (int i = j + 1; i < R; ++i) {
-        acc sm = start(make(0.0f));
-#pragma unroll
-        for (int k = j + 1; k <= i; ++k) add_prod(sm, v[k * R + i], v[j * R + k]);
-        t[i] = mul(finish(sm), najj);
+      for (int j = 0; j < R; ++j) {
+        if (j >= rows) break;
+        ok &= v[j * R + j].hi != 0.0f;
+        v[j * R + j] = rcp(v[j * R + j]);
       }
-#pragma unroll
-      for (int i = j + 1; i < R; ++i)
-        if (i < rows) v[j * R + i] = t[i];
-      v[j * R + j] = ajj;
     }
     return ok;
   }
 
-  /* col <- V col on the first `rows` entries (V is zero past `rows`, so the
-   * sums need no guards) */
+  /* col <- V col on the first `rows` entries */
   __device__ __forceinline__ void apply(ukg_df::df (&col)[R]) const
   {
     using namespace ukg_df;
-    df t[R];
+    if (mode == 2) { /* forward substitution, each entry one compensated dot product */
 #pragma unroll
-    for (int i = R - 1; i >= 0; --i) {
-      acc sm = start(make(0.0f));
+      for (int i = 0; i < R; ++i) {
+        if (i >= rows) break;
+        acc sm = start(col[i]);
 #pragma unroll
-      for (int j = 0; j <= i; ++j) add_prod(sm, v[j * R + i], col[j]);
-      if (full)
+        for (int j = 0; j < i; ++j) add_prod(sm, neg(v[j * R + i]), col[j]);
+        col[i] = mul(finish(sm), v[i * R + i]);
+      }
+    } else if (mode == 1) {
 #pragma unroll
-        for (int j = i + 1; j < R; ++j) add_prod(sm, v[j * R + i], col[j]);
-      t[i] = finish(sm);
+      for (int i = 0; i < R; ++i)
+        if (i < rows) col[i] = mul(col[i], v[i * R + i]);
+    } else {
+      df t[R];
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        acc sm = start(make(0.0f));
+#pragma unroll
+        for (int j = 0; j < R; ++j)
+          if (i < rows && j < rows) add_prod(sm, v[j * R + i], col[j]);
+        t[i] = finish(sm);
+      }
+#pragma unroll
+      for (int i = 0; i < R; ++i) col[i] = t[i];
     }
-#pragma unroll
-    for (int i = 0; i < R; ++i) col[i] = t[i];
   }
 };
 
@@ -771,7 +781,8 @@ __global__ void __launch_bounds__(kWeighBS) weigh_df_kernel(Args<float, float> a
             df col[MX];
 #pragma unroll
             for (int r = 0; r < MX; ++r) {
-              col[r] = r < rows ? split(mine[cc * ld + r]) : make(0.0f);
+              col[r] = make(0.0f);
+              if (r < rows) col[r] = split(mine[cc * ld + r]);
               if (negate) col[r] = neg(col[r]);
             }
             V.apply(col);
