@@ -1146,6 +1146,264 @@ __global__ void __launch_bounds__(128) pair_reg_kernel(Args<float, float> a, int
 }
 
 /* ---------------------------------------------------------------------------
+ * FP32 pair elimination with the pair's inputs staged asynchronously.
+ * Each thread copies its pair's level equations into its own slice of shared
+ * memory with 4-byte cp.async copies in four commit groups (stage A's pivot,
+ * the H_{j+1} columns, stage C's rows, stage B's blocks), so every input of
+ * the pair is in flight at once and stage A starts when its group lands.  The
+ * intermediates (R~, rhs~, Y~, H~, o~) stay in the slice, over inputs already
+ * consumed; records and the next level are written once.  Element e of
+ * thread t's slice is at smem[e * BP + t] (no bank conflicts).  Same
+ * arithmetic as pair_reg_kernel.
+ * ------------------------------------------------------------------------ */
+__device__ __forceinline__ void cp_async4(float* dst, const float* src)
+{
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int G>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(G) : "memory"); }
+
+template <int N, int BP>
+struct PairSlice {
+  static constexpr int NN = N * N, GW = N * N;   /* MX == N */
+  static constexpr int Gj = 0, oj = GW, Hj = GW + N, Fj = Hj + NN, cj = Fj + NN;
+  static constexpr int G1 = cj + N, o1 = G1 + GW, H1 = o1 + N, F1 = H1 + NN, c1 = F1 + NN;
+  static constexpr int width = c1 + N;
+  /* intermediates: R~ over G_j, rhs~ over o_j, Y~ over F_{j+1}, H~ over the
+   * consumed H_{j+1} columns, o~ over c_{j+1} */
+  static constexpr int Rt = Gj, rt = oj, Yt = F1, Ht = H1, ot = c1;
+  float* t0;
+  __device__ __forceinline__ float& operator[](int e) const { return t0[e * BP]; }
+};
+
+template <int N, int BP, int RA>
+__device__ __forceinline__ void ss_stage_a(const PairSlice<N, BP>& S)
+{
+  using L = PairSlice<N, BP>;
+  constexpr int MJ = RA - N;
+  float P[N][RA], v[RA], tau[N];
+  cp_async_wait<3>();
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+#pragma unroll
+    for (int i = 0; i < MJ; ++i) P[q][i] = S[L::Gj + q * N + i];
+#pragma unroll
+    for (int i = 0; i < N; ++i) P[q][MJ + i] = S[L::F1 + q * N + i];
+  }
+#pragma unroll
+  for (int i = 0; i < MJ; ++i) v[i] = S[L::oj + i];
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[MJ + i] = S[L::c1 + i];
+  hh_reg<RA, N>(P, tau);
+  apply_reg<RA, N>(P, tau, v);
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < N; ++i) S[L::Rt + q * N + i] = (i <= q) ? P[q][i] : 0.0f;
+#pragma unroll
+  for (int i = 0; i < N; ++i) S[L::rt + i] = v[i];
+#pragma unroll
+  for (int i = 0; i < MJ; ++i) S[L::ot + i] = v[N + i];
+  cp_async_wait<2>();
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    float col[RA];
+#pragma unroll
+    for (int i = 0; i < MJ; ++i) col[i] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < N; ++i) col[MJ + i] = S[L::H1 + q * N + i];
+    apply_reg<RA, N>(P, tau, col);
+#pragma unroll
+    for (int i = 0; i < N; ++i) S[L::Yt + q * N + i] = col[i];
+#pragma unroll
+    for (int i = 0; i < MJ; ++i) S[L::Ht + q * N + i] = col[N + i];
+  }
+}
+
+template <int N, int BP, int RC>
+__device__ __forceinline__ void ss_stage_c(const PairSlice<N, BP>& S, const Eq<float>& Nx, int64_t sn, int mj)
+{
+  using L = PairSlice<N, BP>;
+  float P[N][RC], v[RC], tau[N];
+  cp_async_wait<1>();
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < RC; ++i) P[q][i] = i < mj ? S[L::Ht + q * N + i] : S[L::G1 + q * N + (i - mj)];
+#pragma unroll
+  for (int i = 0; i < RC; ++i) v[i] = i < mj ? S[L::ot + i] : S[L::o1 + (i - mj)];
+  hh_reg<RC, N>(P, tau);
+  apply_reg<RC, N>(P, tau, v);
+  constexpr int G = RC < N ? RC : N;
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < G; ++i) Nx.G.at(q * N + i, sn) = (i <= q) ? P[q][i] : 0.0f;
+#pragma unroll
+  for (int i = 0; i < G; ++i) Nx.o.at(i, sn) = v[i];
+  Nx.m[sn] = G;
+}
+
+template <int N, int BP>
+__device__ __forceinline__ void ss_stage_b(const PairSlice<N, BP>& S, const Eq<float>& Nx, const Rec<float>& Rr,
+                                           int64_t sn, int64_t se)
+{
+  using L = PairSlice<N, BP>;
+  constexpr int R2 = 2 * N;
+  float P[N][R2], v[R2], tau[N];
+  cp_async_wait<0>();
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      P[q][i] = S[L::Hj + q * N + i];
+      P[q][N + i] = S[L::Rt + q * N + i];
+    }
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    v[i] = S[L::cj + i];
+    v[N + i] = S[L::rt + i];
+  }
+  hh_reg<R2, N>(P, tau);
+  apply_reg<R2, N>(P, tau, v);
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < N; ++i) Rr.R.at(q * N + i, se) = (i <= q) ? P[q][i] : 0.0f;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    Rr.rhs.at(i, se) = v[i];
+    Nx.c.at(i, sn) = v[N + i];
+  }
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    float col[R2];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      col[i] = S[L::Fj + q * N + i];
+      col[N + i] = 0.0f;
+    }
+    apply_reg<R2, N>(P, tau, col);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Rr.Ft.at(q * N + i, se) = col[i];
+      Nx.F.at(q * N + i, sn) = col[N + i];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    float col[R2];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      col[i] = 0.0f;
+      col[N + i] = S[L::Yt + q * N + i];
+    }
+    apply_reg<R2, N>(P, tau, col);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Rr.Y.at(q * N + i, se) = col[i];
+      Nx.H.at(q * N + i, sn) = col[N + i];
+    }
+  }
+}
+
+template <int N, int BP, int RA = N>
+__device__ __forceinline__ void ss_dispatch_a(int ra, const PairSlice<N, BP>& S)
+{
+  if constexpr (RA <= 2 * N) {
+    if (ra == RA) ss_stage_a<N, BP, RA>(S);
+    else ss_dispatch_a<N, BP, RA + 1>(ra, S);
+  }
+}
+
+template <int N, int BP, int RC = 1>
+__device__ __forceinline__ void ss_dispatch_c(int rc, const PairSlice<N, BP>& S, const Eq<float>& Nx, int64_t sn,
+                                              int mj)
+{
+  if constexpr (RC <= 2 * N) {
+    if (rc == RC) ss_stage_c<N, BP, RC>(S, Nx, sn, mj);
+    else ss_dispatch_c<N, BP, RC + 1>(rc, S, Nx, sn, mj);
+  }
+}
+
+constexpr int kPairSsBP = 64;
+
+template <int N>
+__global__ void __launch_bounds__(kPairSsBP) pair_ss_kernel(Args<float, float> a, int)
+{
+  using L = PairSlice<N, kPairSsBP>;
+  extern __shared__ __align__(16) float ss_smem[];
+  const int64_t item = (int64_t)blockIdx.x * kPairSsBP + threadIdx.x;
+  if (item >= a.ct.npairs) return;
+  const int t = find_track(a.ct.pair, a.ntracks, item);
+  const int64_t p = item - a.ct.pair[t];
+  const int64_t sj = a.ct.slot[t] + 2 * p, sj1 = sj + 1;
+  const int64_t sn = a.nt.slot[t] + p, se = a.ct.solve[t] + p;
+  const Eq<float>& C = a.ce;
+  const int mj = C.m[sj], mj1 = C.m[sj1];
+  const L S{ss_smem + threadIdx.x};
+  auto cp = [&](int e, const Soa<float>& src, int es, int64_t s) { cp_async4(&S[e], &src.at(es, s)); };
+  /* group 0: stage A's pivot and right-hand side */
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i < mj) cp(L::Gj + q * N + i, C.G, q * N + i, sj);
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    if (i < mj) cp(L::oj + i, C.o, i, sj);
+#pragma unroll
+  for (int e = 0; e < N * N; ++e) cp(L::F1 + e, C.F, e, sj1);
+#pragma unroll
+  for (int i = 0; i < N; ++i) cp(L::c1 + i, C.c, i, sj1);
+  cp_async_commit();
+  /* group 1: the H_{j+1} columns */
+#pragma unroll
+  for (int e = 0; e < N * N; ++e) cp(L::H1 + e, C.H, e, sj1);
+  cp_async_commit();
+  /* group 2: stage C's observation rows of step j+1 */
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i < mj1) cp(L::G1 + q * N + i, C.G, q * N + i, sj1);
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+    if (i < mj1) cp(L::o1 + i, C.o, i, sj1);
+  cp_async_commit();
+  /* group 3: stage B's blocks of step j (none for a track's first pair) */
+  if (p > 0) {
+#pragma unroll
+    for (int e = 0; e < N * N; ++e) {
+      cp(L::Hj + e, C.H, e, sj);
+      cp(L::Fj + e, C.F, e, sj);
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) cp(L::cj + i, C.c, i, sj);
+  }
+  cp_async_commit();
+
+  ss_dispatch_a<N, kPairSsBP>(mj + N, S);
+  if (mj + mj1 == 0) a.ne.m[sn] = 0;
+  else ss_dispatch_c<N, kPairSsBP>(mj + mj1, S, a.ne, sn, mj);
+  if (p == 0) { /* no stage B: the record is stage A's */
+    cp_async_wait<0>();
+#pragma unroll
+    for (int e = 0; e < N * N; ++e) {
+      a.cr.R.at(e, se) = S[L::Rt + e];
+      a.cr.Y.at(e, se) = S[L::Yt + e];
+      a.cr.Ft.at(e, se) = 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) a.cr.rhs.at(i, se) = S[L::rt + i];
+    return;
+  }
+  ss_stage_b<N, kPairSsBP>(S, a.ne, a.cr, sn, se);
+}
+
+/* ---------------------------------------------------------------------------
  * odd-length tracks: single last step + fix-up, or the one-step base case
  * ------------------------------------------------------------------------ */
 template <typename T, typename TI>
@@ -2003,7 +2261,8 @@ template <typename T>
 struct Kernels {
   void (*pair)(Args<T, T>, int) = nullptr;
   void (*solve)(Args<T, T>, int) = nullptr;
-  int bp = 0, bs = 0; /* fixed block sizes of the specialised kernels (0: pick) */
+  int bp = 0, bs = 0;     /* fixed block sizes of the specialised kernels (0: pick) */
+  size_t pair_smem = 0;   /* dynamic shared memory of the pair kernel (0: per-thread workspace) */
 };
 
 template <typename T>
@@ -2012,10 +2271,12 @@ Kernels<T> choose_kernels(int n, int mx)
   Kernels<T> k;
   if constexpr (sizeof(T) == sizeof(float)) {
     if (n == mx && (n == 6 || n == 4)) {
-      k.pair = n == 6 ? pair_reg_kernel<6, 6> : pair_reg_kernel<4, 4>;
+      k.pair = n == 6 ? pair_ss_kernel<6> : pair_ss_kernel<4>;
       k.solve = n == 6 ? solve_kernel<T, 6, 64> : solve_kernel<T, 4, 64>;
-      k.bp = 128;
+      k.bp = kPairSsBP;
       k.bs = 64;
+      k.pair_smem = (size_t)kPairSsBP * sizeof(float) *
+                    (n == 6 ? PairSlice<6, kPairSsBP>::width : PairSlice<4, kPairSsBP>::width);
       return k;
     }
   }
@@ -2121,7 +2382,8 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
   cudaFuncSetAttribute(weigh_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bw * pt_weigh));
   if (staged)
     cudaFuncSetAttribute(weigh_staged_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)weigh_smem);
-  cudaFuncSetAttribute(K.pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bp * pt_pair));
+  const size_t pair_smem = K.pair_smem ? K.pair_smem : bp * pt_pair;
+  cudaFuncSetAttribute(K.pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem);
   cudaFuncSetAttribute(tail_kernel<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bt * pt_tail));
   cudaFuncSetAttribute(K.solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bs * pt_solve));
   cudaFuncSetAttribute(residual_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(br * pt_res));
@@ -2197,7 +2459,7 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
     a.ce = l == 0 ? eq0() : eqT(l);
     if (l + 1 < nlev) a.ne = eqT(l + 1);
     if (lp[l].npairs > 0)
-      UKG_LAUNCH(kPair, st, (K.pair<<<grid(lp[l].npairs, bp), bp, bp * pt_pair, st>>>(a, rmax)));
+      UKG_LAUNCH(kPair, st, (K.pair<<<grid(lp[l].npairs, bp), bp, pair_smem, st>>>(a, rmax)));
     if (lp[l].ntail > 0)
       UKG_LAUNCH(UKG_K_TAIL, st, (tail_kernel<T, T><<<grid(lp[l].ntail, bt), bt, bt * pt_tail, st>>>(a)));
   }
