@@ -1207,8 +1207,8 @@ __device__ __forceinline__ void ss_stage_a(const PairSlice<N, BP>& S)
 #pragma unroll
   for (int i = 0; i < MJ; ++i) S[L::ot + i] = v[N + i];
   cp_async_wait<2>();
-#pragma unroll
-  for (int q = 0; q < N; ++q) {
+#pragma unroll 1
+  for (int q = 0; q < N; ++q) { /* not unrolled: keeps the kernel's code small */
     float col[RA];
 #pragma unroll
     for (int i = 0; i < MJ; ++i) col[i] = 0.0f;
@@ -1277,7 +1277,7 @@ __device__ __forceinline__ void ss_stage_b(const PairSlice<N, BP>& S, const Eq<f
     Rr.rhs.at(i, se) = v[i];
     Nx.c.at(i, sn) = v[N + i];
   }
-#pragma unroll
+#pragma unroll 1
   for (int q = 0; q < N; ++q) {
     float col[R2];
 #pragma unroll
@@ -1292,7 +1292,7 @@ __device__ __forceinline__ void ss_stage_b(const PairSlice<N, BP>& S, const Eq<f
       Nx.F.at(q * N + i, sn) = col[N + i];
     }
   }
-#pragma unroll
+#pragma unroll 1
   for (int q = 0; q < N; ++q) {
     float col[R2];
 #pragma unroll
