@@ -1515,6 +1515,199 @@ __global__ void tail_kernel(Args<T, TI> a)
 }
 
 /* ---------------------------------------------------------------------------
+ * FP32 tail work (states only) with register-resident blocks: the same
+ * arithmetic as tail_kernel, each QR an instantiation with compile-time rows
+ * (dispatched on the run-time row count).  Hand-offs between the stages (R~
+ * and o' of the single step's observation, its leftover rows Z and o'') go
+ * through a per-thread slice of shared memory, element e at [e*32 + lane].
+ * ------------------------------------------------------------------------ */
+constexpr int kTailBS = 32;
+
+template <int N>
+struct TailSlice {
+  static constexpr int Rt = 0, op = N * N, Z = N * N + N, opp = 2 * N * N + N, width = 2 * N * N + 2 * N;
+  float* t0;
+  __device__ __forceinline__ float& operator[](int e) const { return t0[e * kTailBS]; }
+};
+
+/* observation QR of the single last step: [G_s | o_s], MS rows */
+template <int N, int MS>
+__device__ __forceinline__ void tail_obs(const Eq<float>& C, int64_t s, const TailSlice<N>& S)
+{
+  float P[N][MS], v[MS], tau[N];
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < MS; ++i) P[q][i] = C.G.at(q * N + i, s);
+#pragma unroll
+  for (int i = 0; i < MS; ++i) v[i] = C.o.at(i, s);
+  hh_reg<MS, N>(P, tau);
+  apply_reg<MS, N>(P, tau, v);
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < MS; ++i) S[TailSlice<N>::Rt + q * N + i] = (i <= q) ? P[q][i] : 0.0f;
+#pragma unroll
+  for (int i = 0; i < MS; ++i) S[TailSlice<N>::op + i] = v[i];
+}
+
+/* evolution QR of the single last step: [H_s F_s c_s; R~ 0 o'], N+MT rows */
+template <int N, int MT>
+__device__ __forceinline__ void tail_evo(const Eq<float>& C, const Rec<float>& Rr, int64_t s, int64_t es,
+                                         const TailSlice<N>& S)
+{
+  using L = TailSlice<N>;
+  constexpr int R = N + MT;
+  float P[N][R], v[R], tau[N];
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) P[q][i] = C.H.at(q * N + i, s);
+#pragma unroll
+    for (int i = 0; i < MT; ++i) P[q][N + i] = (i <= q) ? S[L::Rt + q * N + i] : 0.0f;
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[i] = C.c.at(i, s);
+#pragma unroll
+  for (int i = 0; i < MT; ++i) v[N + i] = S[L::op + i];
+  hh_reg<R, N>(P, tau);
+  apply_reg<R, N>(P, tau, v);
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      Rr.R.at(q * N + i, es) = (i <= q) ? P[q][i] : 0.0f;
+      Rr.Y.at(q * N + i, es) = 0.0f;
+    }
+#pragma unroll
+  for (int i = 0; i < N; ++i) Rr.rhs.at(i, es) = v[i];
+#pragma unroll
+  for (int i = 0; i < MT; ++i) S[L::opp + i] = v[N + i];
+#pragma unroll 1
+  for (int q = 0; q < N; ++q) {
+    float col[R];
+#pragma unroll
+    for (int i = 0; i < N; ++i) col[i] = C.F.at(q * N + i, s);
+#pragma unroll
+    for (int i = 0; i < MT; ++i) col[N + i] = 0.0f;
+    apply_reg<R, N>(P, tau, col);
+#pragma unroll
+    for (int i = 0; i < N; ++i) Rr.Ft.at(q * N + i, es) = col[i];
+#pragma unroll
+    for (int i = 0; i < MT; ++i) S[L::Z + q * N + i] = col[N + i];
+  }
+}
+
+/* fix-up: QR of [G~ o (gp rows of the next level's slot); Z o''], RF rows */
+template <int N, int RF>
+__device__ __forceinline__ void tail_fix(const Eq<float>& Nx, int64_t sn, int gp, const TailSlice<N>& S)
+{
+  using L = TailSlice<N>;
+  float P[N][RF], v[RF], tau[N];
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < RF; ++i) P[q][i] = i < gp ? Nx.G.at(q * N + i, sn) : S[L::Z + q * N + (i - gp)];
+#pragma unroll
+  for (int i = 0; i < RF; ++i) v[i] = i < gp ? Nx.o.at(i, sn) : S[L::opp + (i - gp)];
+  hh_reg<RF, N>(P, tau);
+  apply_reg<RF, N>(P, tau, v);
+  constexpr int G2 = RF < N ? RF : N;
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+#pragma unroll
+    for (int i = 0; i < G2; ++i) Nx.G.at(q * N + i, sn) = (i <= q) ? P[q][i] : 0.0f;
+#pragma unroll
+  for (int i = 0; i < G2; ++i) Nx.o.at(i, sn) = v[i];
+  Nx.m[sn] = G2;
+}
+
+template <int N, int K = 1>
+__device__ __forceinline__ void tail_obs_d(int ms, const Eq<float>& C, int64_t s, const TailSlice<N>& S)
+{
+  if constexpr (K <= N) {
+    if (ms == K) tail_obs<N, K>(C, s, S);
+    else tail_obs_d<N, K + 1>(ms, C, s, S);
+  }
+}
+template <int N, int K = 0>
+__device__ __forceinline__ void tail_evo_d(int mt, const Eq<float>& C, const Rec<float>& Rr, int64_t s, int64_t es,
+                                           const TailSlice<N>& S)
+{
+  if constexpr (K <= N) {
+    if (mt == K) tail_evo<N, K>(C, Rr, s, es, S);
+    else tail_evo_d<N, K + 1>(mt, C, Rr, s, es, S);
+  }
+}
+template <int N, int K = 1>
+__device__ __forceinline__ void tail_fix_d(int rf, const Eq<float>& Nx, int64_t sn, int gp, const TailSlice<N>& S)
+{
+  if constexpr (K <= 2 * N) {
+    if (rf == K) tail_fix<N, K>(Nx, sn, gp, S);
+    else tail_fix_d<N, K + 1>(rf, Nx, sn, gp, S);
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(kTailBS) tail_reg_kernel(Args<float, float> a)
+{
+  __shared__ float tail_smem[TailSlice<N>::width * kTailBS];
+  const int64_t item = (int64_t)blockIdx.x * kTailBS + threadIdx.x;
+  if (item >= a.ct.ntail) return;
+  const Eq<float>& C = a.ce;
+  const int t = (int)a.ct.tail[item];
+  const int64_t L = a.ct.L[t];
+  const int64_t sb = a.ct.slot[t];
+  if (L == 1) { /* base case: x = R^{-1} Q^T o */
+    const int m0 = C.m[sb];
+    double* x = a.state + orig_step(a.track_start, a.level, t, 0) * N;
+    if (m0 < N) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) x[i] = NAN;
+      atomicOr(a.flag, 2);
+      return;
+    }
+    float P[N][N], v[N], tau[N];
+#pragma unroll
+    for (int q = 0; q < N; ++q)
+#pragma unroll
+      for (int i = 0; i < N; ++i) P[q][i] = C.G.at(q * N + i, sb);
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = C.o.at(i, sb);
+    hh_reg<N, N>(P, tau);
+    apply_reg<N, N>(P, tau, v);
+    bool bad = false;
+    if (a.baseR.p)
+#pragma unroll
+      for (int q = 0; q < N; ++q)
+#pragma unroll
+        for (int i = 0; i < N; ++i) a.baseR.at(q * N + i, t) = (i <= q) ? P[q][i] : 0.0f;
+#pragma unroll
+    for (int i = N - 1; i >= 0; --i) {
+      float sm = v[i];
+#pragma unroll
+      for (int k = i + 1; k < N; ++k) sm = fmaf(-P[k][i], v[k], sm);
+      bad |= P[i][i] == 0.0f;
+      v[i] = sm * (1.0f / P[i][i]);
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) x[i] = ukg_df::f32_to_f64(v[i]);
+    if (bad) atomicOr(a.flag, 2);
+    return;
+  }
+  const TailSlice<N> S{tail_smem + threadIdx.x};
+  const int64_t s = sb + L - 1;
+  const int64_t es = a.ct.solve[t] + (L - 1) / 2;
+  const int64_t sn = a.nt.slot[t] + L / 2 - 1;
+  const int ms = C.m[s], mt = ms < N ? ms : N;
+  if (ms > 0) tail_obs_d<N>(ms, C, s, S);
+  tail_evo_d<N>(mt, C, a.cr, s, es, S);
+  const int gp = a.ne.m[sn], rf = gp + mt;
+  if (rf > 0) tail_fix_d<N>(rf, a.ne, sn, gp, S);
+  else a.ne.m[sn] = 0;
+}
+
+/* ---------------------------------------------------------------------------
  * back-substitution and covariance recurrence for the even steps of a level
  *
  * With B = [Ft Y] and Sigma = [[Smm Smp]; [Smp^T Spp]] the joint covariance of
@@ -2461,7 +2654,18 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
     if (lp[l].npairs > 0)
       UKG_LAUNCH(kPair, st, (K.pair<<<grid(lp[l].npairs, bp), bp, pair_smem, st>>>(a, rmax)));
     if (lp[l].ntail > 0)
-      UKG_LAUNCH(UKG_K_TAIL, st, (tail_kernel<T, T><<<grid(lp[l].ntail, bt), bt, bt * pt_tail, st>>>(a)));
+    {
+      bool done = false;
+      if constexpr (sizeof(T) == sizeof(float)) {
+        if (!want_cov && n == mx && (n == 6 || n == 4)) {
+          auto tk = n == 6 ? tail_reg_kernel<6> : tail_reg_kernel<4>;
+          UKG_LAUNCH(UKG_K_TAIL, st, (tk<<<grid(lp[l].ntail, kTailBS), kTailBS, 0, st>>>(a)));
+          done = true;
+        }
+      }
+      if (!done)
+        UKG_LAUNCH(UKG_K_TAIL, st, (tail_kernel<T, T><<<grid(lp[l].ntail, bt), bt, bt * pt_tail, st>>>(a)));
+    }
   }
   /* ---- back-substitution ---- */
   for (int l = nlev - 2; l >= 0; --l) {
