@@ -692,7 +692,7 @@ struct DfWeights {
 };
 
 template <int N, int MX>
-__global__ void __launch_bounds__(kWeighBS) weigh_df_kernel(Args<float, float> a, Eq<float> lo, RawDev raw,
+__global__ void __launch_bounds__(kWeighBS, 4) weigh_df_kernel(Args<float, float> a, Eq<float> lo, RawDev raw,
                                                             int64_t nsteps, int bulk)
 {
   using namespace ukg_df;
