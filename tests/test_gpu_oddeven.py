@@ -81,6 +81,19 @@ def test_host_and_device_locations_agree():
     np.testing.assert_array_equal(Sd, Sh)
 
 
+@pytest.mark.parametrize("fp32", [False, True])
+def test_host_location_in_pipelined_chunks(fp32):
+    """Host arrays of more than 2^20 steps are staged in chunks of whole tracks
+    (copies overlapped with smoothing); the results equal the device path's."""
+    P = pb.constant_velocity([600000, 600000, 100000, 37], seed=9)
+    cov = not fp32
+    Xd, Sd = native.smooth(P, covariance=cov, fp32_refine=fp32, location="device")
+    Xh, Sh = native.smooth(P, covariance=cov, fp32_refine=fp32, location="host")
+    np.testing.assert_array_equal(Xd, Xh)
+    if cov:
+        np.testing.assert_array_equal(Sd, Sh)
+
+
 def test_no_covariance_gives_same_states():
     P = pb.constant_velocity([77, 5], seed=6)
     X1, S1 = native.smooth(P, covariance=True)

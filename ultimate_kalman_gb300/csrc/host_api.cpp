@@ -21,6 +21,7 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -97,10 +98,25 @@ namespace {
 
 struct Stage {
   int device = -1;
-  void* p = nullptr;
+  void* p = nullptr; /* two staging buffers, back to back */
   size_t bytes = 0;
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  cudaEvent_t h2d_done[2] = {nullptr, nullptr}, computed[2] = {nullptr, nullptr}, d2h_done[2] = {nullptr, nullptr};
 };
-thread_local Stage tl_stage; /* device copy of host-located packed problems */
+thread_local Stage tl_stage; /* device staging of host-located packed problems */
+
+void stage_release(Stage& S)
+{
+  if (S.p) cudaFree(S.p);
+  for (int b = 0; b < 2; ++b) {
+    if (S.h2d_done[b]) cudaEventDestroy(S.h2d_done[b]);
+    if (S.computed[b]) cudaEventDestroy(S.computed[b]);
+    if (S.d2h_done[b]) cudaEventDestroy(S.d2h_done[b]);
+  }
+  if (S.h2d) cudaStreamDestroy(S.h2d);
+  if (S.d2h) cudaStreamDestroy(S.d2h);
+  S = Stage();
+}
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -118,64 +134,125 @@ int device_ready()
 
 typedef int (*device_smoother)(uint32_t, const kalman_gpu_problem_t*, void*);
 
-/* Runs a device smoother on a packed problem held in host memory: copies the
- * inputs into a cached device buffer, runs, copies the outputs back.         */
+/* Runs a device smoother on a packed problem held in host memory.  The tracks
+ * are cut into chunks of about a sixteenth of the steps (at least 2^20 steps
+ * a chunk); chunk k's inputs are copied into staging buffer k mod 2 on a copy
+ * stream while chunk k-1 is smoothed on the caller's stream, and its states
+ * (and covariances) are copied back on a second copy stream while chunk k+1
+ * is smoothed -- so the host link, which bounds this path, stays busy.      */
 int run_host_problem(device_smoother fn, uint32_t options, const kalman_gpu_problem_t* p, bool want_cov,
                      cudaStream_t st)
 {
   const int64_t N = p->nsteps, n = p->n, mm = p->mmax;
-  const size_t sz[] = {
-      (size_t)(N * n * n * 8), (size_t)(N * n * n * 8), (size_t)(N * n * 8), (size_t)(N * n * n * 8), (size_t)N,
-      (size_t)(N * mm * n * 8), (size_t)(N * mm * 8), (size_t)(N * mm * mm * 8), (size_t)N, (size_t)(N * 4),
-      (size_t)(N * n * 8), want_cov ? (size_t)(N * n * n * 8) : 0};
-  const void* src[] = {p->H, p->F, p->c, p->K, p->K_type, p->G, p->o, p->C, p->C_type, p->obs_rows};
-  size_t off[12], total = 0;
+  /* chunks of whole tracks */
+  const int64_t target = std::max<int64_t>(N / 16, (int64_t)1 << 20);
+  std::vector<int> cut{0};
+  for (int t = 1; t < p->ntracks; ++t)
+    if (p->track_start[t] - p->track_start[cut.back()] >= target) cut.push_back(t);
+  cut.push_back(p->ntracks);
+  const int nchunks = (int)cut.size() - 1;
+  int64_t cmax = 0;
+  for (int k = 0; k < nchunks; ++k)
+    cmax = std::max<int64_t>(cmax, p->track_start[cut[k + 1]] - p->track_start[cut[k]]);
+
+  /* bytes per step of each array: H F c K K_type G o C C_type obs_rows | state cov */
+  const size_t per[12] = {(size_t)(n * n * 8), (size_t)(n * n * 8), (size_t)(n * 8), (size_t)(n * n * 8), 1,
+                          (size_t)(mm * n * 8), (size_t)(mm * 8), (size_t)(mm * mm * 8), 1, 4, (size_t)(n * 8),
+                          want_cov ? (size_t)(n * n * 8) : 0};
+  const void* src[10] = {p->H, p->F, p->c, p->K, p->K_type, p->G, p->o, p->C, p->C_type, p->obs_rows};
+  size_t off[12], half = 0;
   for (int i = 0; i < 12; ++i) {
-    off[i] = total;
-    total = align_up(total + sz[i], 256);
+    off[i] = half;
+    half = align_up(half + per[i] * (size_t)cmax, 256);
   }
   int dev = 0;
   cudaGetDevice(&dev);
   Stage& S = tl_stage;
-  if (S.p && (S.bytes < total || S.device != dev)) {
-    cudaFree(S.p);
-    S = Stage();
-  }
+  if (S.p && (S.bytes < 2 * half || S.device != dev)) stage_release(S);
   if (!S.p) {
-    cudaError_t e = cudaMalloc(&S.p, total);
+    cudaError_t e = cudaMalloc(&S.p, 2 * half);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S.h2d, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S.d2h, cudaStreamNonBlocking);
+    for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+      e = cudaEventCreateWithFlags(&S.h2d_done[b], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S.computed[b], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S.d2h_done[b], cudaEventDisableTiming);
+    }
     if (e != cudaSuccess) {
       cudaGetLastError();
-      S = Stage();
-      return ukg_set_error(KALMAN_GPU_ENOMEM, "cudaMalloc of %zu bytes for the problem failed", total);
+      stage_release(S);
+      return ukg_set_error(KALMAN_GPU_ENOMEM, "staging %zu bytes of the problem on the device failed: %s",
+                           2 * half, cudaGetErrorString(e));
     }
-    S.bytes = total;
+    S.bytes = 2 * half;
     S.device = dev;
   }
-  char* D = (char*)S.p;
-  for (int i = 0; i < 10; ++i)
-    if (sz[i] && src[i]) cudaMemcpyAsync(D + off[i], src[i], sz[i], cudaMemcpyHostToDevice, st);
-  kalman_gpu_problem_t d = *p;
-  d.location = KALMAN_GPU_DEVICE;
-  d.H = (const double*)(D + off[0]);
-  d.F = (const double*)(D + off[1]);
-  d.c = (const double*)(D + off[2]);
-  d.K = (const double*)(D + off[3]);
-  d.K_type = (const char*)(D + off[4]);
-  d.G = (const double*)(D + off[5]);
-  d.o = (const double*)(D + off[6]);
-  d.C = (const double*)(D + off[7]);
-  d.C_type = (const char*)(D + off[8]);
-  d.obs_rows = (const int32_t*)(D + off[9]);
-  d.state = (double*)(D + off[10]);
-  d.covariance = want_cov ? (double*)(D + off[11]) : nullptr;
-  int status = fn(options, &d, st);
-  if (status != KALMAN_GPU_ECUDA) {
-    cudaMemcpyAsync(p->state, d.state, sz[10], cudaMemcpyDeviceToHost, st);
-    if (want_cov) cudaMemcpyAsync(p->covariance, d.covariance, sz[11], cudaMemcpyDeviceToHost, st);
-    cudaError_t e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return ukg_set_error(KALMAN_GPU_ECUDA, "copying results back: %s", cudaGetErrorString(e));
+  /* the events of an earlier call are complete: that call synchronized */
+  auto buffer = [&](int b) { return (char*)S.p + (size_t)b * half; };
+  auto copy_in = [&](int k) {
+    const int64_t g0 = p->track_start[cut[k]], g1 = p->track_start[cut[k + 1]];
+    char* D = buffer(k & 1);
+    for (int i = 0; i < 10; ++i)
+      if (per[i] && src[i])
+        cudaMemcpyAsync(D + off[i], (const char*)src[i] + (size_t)g0 * per[i], (size_t)(g1 - g0) * per[i],
+                        cudaMemcpyHostToDevice, S.h2d);
+    cudaEventRecord(S.h2d_done[k & 1], S.h2d);
+  };
+  bool used[2] = {false, false};
+  int status = 0;
+  char first_error[512] = "";
+  copy_in(0);
+  for (int k = 0; k < nchunks; ++k) {
+    if (k + 1 < nchunks) copy_in(k + 1); /* overlaps this chunk's smoothing */
+    const int b = k & 1;
+    const int64_t g0 = p->track_start[cut[k]], g1 = p->track_start[cut[k + 1]];
+    std::vector<int64_t> ts(cut[k + 1] - cut[k] + 1);
+    for (size_t i = 0; i < ts.size(); ++i) ts[i] = p->track_start[cut[k] + (int)i] - g0;
+    char* D = buffer(b);
+    kalman_gpu_problem_t d = *p;
+    d.location = KALMAN_GPU_DEVICE;
+    d.ntracks = cut[k + 1] - cut[k];
+    d.nsteps = g1 - g0;
+    d.track_start = ts.data();
+    d.H = (const double*)(D + off[0]);
+    d.F = (const double*)(D + off[1]);
+    d.c = (const double*)(D + off[2]);
+    d.K = (const double*)(D + off[3]);
+    d.K_type = (const char*)(D + off[4]);
+    d.G = (const double*)(D + off[5]);
+    d.o = (const double*)(D + off[6]);
+    d.C = (const double*)(D + off[7]);
+    d.C_type = (const char*)(D + off[8]);
+    d.obs_rows = (const int32_t*)(D + off[9]);
+    d.state = (double*)(D + off[10]);
+    d.covariance = want_cov ? (double*)(D + off[11]) : nullptr;
+    cudaStreamWaitEvent(st, S.h2d_done[b], 0);
+    if (used[b]) cudaStreamWaitEvent(st, S.d2h_done[b], 0); /* chunk k-2's outputs are read back */
+    const int s = fn(options, &d, st);                    /* returns after the smoothing completed */
+    if (s == KALMAN_GPU_ECUDA) {
+      cudaStreamSynchronize(S.h2d);
+      cudaStreamSynchronize(S.d2h);
+      return s;
+    }
+    if (s && !status) {
+      status = s;
+      snprintf(first_error, sizeof(first_error), "%s", kalman_gpu_last_error());
+    }
+    cudaEventRecord(S.computed[b], st);
+    cudaStreamWaitEvent(S.d2h, S.computed[b], 0);
+    cudaMemcpyAsync((char*)p->state + (size_t)g0 * per[10], d.state, (size_t)(g1 - g0) * per[10],
+                    cudaMemcpyDeviceToHost, S.d2h);
+    if (want_cov)
+      cudaMemcpyAsync((char*)p->covariance + (size_t)g0 * per[11], d.covariance, (size_t)(g1 - g0) * per[11],
+                      cudaMemcpyDeviceToHost, S.d2h);
+    cudaEventRecord(S.d2h_done[b], S.d2h);
+    used[b] = true;
   }
-  return status;
+  cudaError_t e = cudaStreamSynchronize(S.d2h);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(S.h2d);
+  if (e != cudaSuccess) return ukg_set_error(KALMAN_GPU_ECUDA, "copying the problem: %s", cudaGetErrorString(e));
+  if (status) return ukg_set_error(status, "%s", first_error);
+  return 0;
 }
 
 int smooth_packed(device_smoother fn, uint32_t options, const kalman_gpu_problem_t* p, void* stream)
@@ -210,8 +287,7 @@ extern "C" void kalman_gpu_release(void)
 {
   ukg_release_oddeven_workspace();
   ukg_release_associative_workspace();
-  if (tl_stage.p) cudaFree(tl_stage.p);
-  tl_stage = Stage();
+  stage_release(tl_stage);
 }
 
 /* -------------------------------------------------------------------------- */

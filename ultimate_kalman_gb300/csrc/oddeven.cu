@@ -2497,9 +2497,22 @@ Kernels<T> choose_kernels(int n, int mx)
 
 /* Uploads the tables, runs every kernel of the smoother on stream st using
  * the device workspace at B (at least P.bytes), waits, reports the flags.   */
+/* copies the plan tables from page-locked, device-mapped host memory: a kernel
+ * rather than a DMA, so the upload never queues behind large copies of the
+ * caller's arrays on a copy engine (the host path overlaps those with
+ * smoothing) */
+__global__ void upload_tables_kernel(int64_t* __restrict__ dst, const int64_t* __restrict__ src, int64_t count)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+/* tab_dev: the device address of tab when tab is page-locked and mapped (the
+ * tables are then uploaded by a kernel); null: tab is ordinary host memory
+ * (uploaded with cudaMemcpyAsync) */
 template <typename T>
 int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, const Plan& P, const int64_t* tab,
-             char* B)
+             char* B, const int64_t* tab_dev = nullptr)
 {
   const int n = p->n, T_ = p->ntracks, nlev = P.nlev;
   const int mx = p->mmax > n ? p->mmax : n;
@@ -2508,7 +2521,11 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
   const LevelPlan* lp = P.lp;
   int64_t* dtab = (int64_t*)(B + P.o_tab);
   int* dflag = (int*)(B + P.o_flag);
-  cudaMemcpyAsync(dtab, tab, P.tab_entries * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+  if (tab_dev)
+    upload_tables_kernel<<<(unsigned)std::min<size_t>((P.tab_entries + 255) / 256, 1024), 256, 0, st>>>(
+        dtab, tab_dev, (int64_t)P.tab_entries);
+  else
+    cudaMemcpyAsync(dtab, tab, P.tab_entries * sizeof(int64_t), cudaMemcpyHostToDevice, st);
   cudaMemsetAsync(dflag, 0, sizeof(int), st);
 
   auto tables = [&](int l) {
@@ -2768,7 +2785,36 @@ struct Workspace {
   size_t dev_bytes = 0;
 };
 thread_local Workspace tl_ws; /* one cached device arena per host thread */
-thread_local std::vector<int64_t> tl_tab;
+
+/* page-locked, device-mapped host buffer for the plan tables (one per host
+ * thread; every call waits for its kernels, so the next call may refill it) */
+struct MappedTables {
+  int64_t* host = nullptr;
+  int64_t* dev = nullptr;
+  size_t entries = 0;
+};
+thread_local MappedTables tl_mtab;
+
+int ensure_mapped_tables(size_t entries)
+{
+  MappedTables& m = tl_mtab;
+  if (m.entries < entries) {
+    if (m.host) cudaFreeHost(m.host);
+    m = MappedTables();
+    const size_t want = std::max<size_t>(entries, 1 << 16);
+    cudaError_t e = cudaHostAlloc((void**)&m.host, want * sizeof(int64_t), cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&m.dev, m.host, 0);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      if (m.host) cudaFreeHost(m.host);
+      m = MappedTables();
+      return ukg_set_error(KALMAN_GPU_ENOMEM, "page-locked plan tables (%zu entries): %s", entries,
+                           cudaGetErrorString(e));
+    }
+    m.entries = want;
+  }
+  return 0;
+}
 
 int ensure_workspace(size_t bytes, void** out)
 {
@@ -2801,6 +2847,8 @@ extern "C" void ukg_release_oddeven_workspace(void)
 {
   if (tl_ws.dev) cudaFree(tl_ws.dev);
   tl_ws = Workspace();
+  if (tl_mtab.host) cudaFreeHost(tl_mtab.host);
+  tl_mtab = MappedTables();
 }
 
 extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream)
@@ -2811,12 +2859,13 @@ extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* 
   Plan P;
   const size_t need = build_plan(p, want_cov, fp32, fp32, P, nullptr, 0);
   if (need == 0) return ukg_set_error(KALMAN_GPU_EINVAL, "tracks longer than 2^%d steps", kMaxLevels - 1);
-  tl_tab.resize(need);
-  build_plan(p, want_cov, fp32, fp32, P, tl_tab.data(), need);
+  if (int e = ensure_mapped_tables(need)) return e;
+  int64_t* tab = tl_mtab.host;
+  build_plan(p, want_cov, fp32, fp32, P, tab, need);
   void* base = nullptr;
   if (int e = ensure_workspace(P.bytes, &base)) return e;
-  if (fp32) return run_plan<float>(options, p, (cudaStream_t)cuda_stream, P, tl_tab.data(), (char*)base);
-  return run_plan<double>(options, p, (cudaStream_t)cuda_stream, P, tl_tab.data(), (char*)base);
+  if (fp32) return run_plan<float>(options, p, (cudaStream_t)cuda_stream, P, tab, (char*)base, tl_mtab.dev);
+  return run_plan<double>(options, p, (cudaStream_t)cuda_stream, P, tab, (char*)base, tl_mtab.dev);
 }
 
 /* ---------------------------------------------------------------------------
