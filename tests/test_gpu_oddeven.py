@@ -132,3 +132,23 @@ def test_malformed_observation_rows_on_device():
     with pytest.raises(native.KalmanError) as e:
         native.smooth(P, location="device")
     assert e.value.status == 1
+
+
+@pytest.mark.parametrize("n,k", [(9, 41), (12, 300), (24, 120), (48, 40)])
+def test_larger_states_cta_path(n, k):
+    """State dimensions past 8 run one thread block per item: parity with the
+    oracle (states and covariances), with missing observations and tracks of
+    length 1 and 2."""
+    P = pb.random_dynamics([k, 37, 1, 2], n, n // 2, seed=4 + n, per_step=True, missing=0.1)
+    X, S = native.smooth(P)
+    check(P, X, S)
+
+
+def test_config4_shape_n128():
+    """n = 128, m = 64 (the largest shape this build accepts), all covariance
+    types of the reference in one problem."""
+    P = pb.random_dynamics([23, 6], 128, 64, seed=21, per_step=True, K_type="W", C_type="U")
+    X, S = native.smooth(P)
+    check(P, X, S)
+    X2, _ = native.smooth(P, covariance=False, fp32_refine=True)
+    assert oracle.rel_err_states(X2, X) < 1e-11

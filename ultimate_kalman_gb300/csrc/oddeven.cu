@@ -2274,6 +2274,8 @@ __global__ void add_kernel(double* x, const double* d, int64_t count)
   if (g < count) x[g] += d[g];
 }
 
+#include "oddeven_cta.cuh"
+
 /* ---------------------------------------------------------------------------
  * host side: plan, workspace, launches
  * ------------------------------------------------------------------------ */
@@ -2851,10 +2853,161 @@ extern "C" void ukg_release_oddeven_workspace(void)
   tl_mtab = MappedTables();
 }
 
+/* ---------------------------------------------------------------------------
+ * larger state dimensions: one CTA per item (oddeven_cta.cuh), FP64
+ * ------------------------------------------------------------------------ */
+constexpr int kCtaMinN = 9; /* per-thread kernels below, CTA kernels from here on */
+constexpr int kCtaMaxN = 128;
+
+int64_t cta_scratch_per_cta(int n, int mmax)
+{
+  const int64_t rmax = std::max(n, mmax);
+  const int64_t weigh = rmax * rmax + rmax * (2 * n + 1) + rmax * cta::NT;
+  const int64_t tail = 7 * (int64_t)n * n + 5 * n + (int64_t)std::max(n, mmax) * (n + 1) + n;
+  const int64_t mx = rmax; /* max(n, mmax) */
+  const int64_t pair = std::max(std::max(2 * (int64_t)n * (3 * n + 1), (mx + n) * (2 * n + 1)), 2 * mx * (n + 1));
+  const int64_t solve = 7 * (int64_t)n * n + n;
+  return std::max(std::max(weigh, tail), std::max(pair, solve)) + 32;
+}
+
+int cta_count()
+{
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return std::max(sms, 1) * 4;
+}
+
+int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, const Plan& P,
+                 const int64_t* tab_dev, char* B, double* scratch, int64_t per_cta, int ncta)
+{
+  const int n = p->n, T_ = p->ntracks, nlev = P.nlev;
+  const int mx = p->mmax > n ? p->mmax : n;
+  const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
+  const int64_t nn = (int64_t)n * n;
+  const LevelPlan* lp = P.lp;
+  int64_t* dtab = (int64_t*)(B + P.o_tab);
+  int* dflag = (int*)(B + P.o_flag);
+  upload_tables_kernel<<<(unsigned)std::min<size_t>((P.tab_entries + 255) / 256, 1024), 256, 0, st>>>(
+      dtab, tab_dev, (int64_t)P.tab_entries);
+  cudaMemsetAsync(dflag, 0, sizeof(int), st);
+  auto tables = [&](int l) {
+    Tables d;
+    memset(&d, 0, sizeof(d));
+    if (l >= nlev) return d;
+    const LevelPlan& L = lp[l];
+    d.L = dtab + L.off_L;
+    d.slot = dtab + L.off_slot;
+    d.pair = dtab + L.off_pair;
+    d.solve = dtab + L.off_solve;
+    d.tail = dtab + L.off_tail;
+    d.npairs = L.npairs;
+    d.nsolve = L.nsolve;
+    d.ntail = L.ntail;
+    return d;
+  };
+  auto eqa = [&](size_t off, size_t off_m, int64_t S) {
+    double* e = (double*)(B + off);
+    cta::EqA<double> d;
+    d.F = {e, nn};
+    d.H = {e + nn * S, nn};
+    d.c = {e + 2 * nn * S, n};
+    d.G = {e + (2 * nn + n) * S, (int64_t)mx * n};
+    d.o = {e + (2 * nn + n + (int64_t)mx * n) * S, mx};
+    d.m = (int32_t*)(B + off_m);
+    return d;
+  };
+  auto eq_level = [&](int l) { /* odd levels in their own region, even levels reuse level 0's */
+    return (l & 1) ? eqa(P.o_eqA, P.o_mA, P.S1) : eqa(P.o_eq0, P.o_m0, P.S0);
+  };
+  auto rec = [&](int l) {
+    cta::RecA<double> r;
+    memset(&r, 0, sizeof(r));
+    if (l >= nlev) return r;
+    const int64_t E = std::max<int64_t>(lp[l].E, 1);
+    double* d = (double*)(B + P.o_rec[l]);
+    r.R = {d, nn};
+    r.Ft = {d + nn * E, nn};
+    r.Y = {d + 2 * nn * E, nn};
+    r.rhs = {d + 3 * nn * E, n};
+    if (want_cov && l > 0) r.U = {(double*)(B + P.o_U[l]), nn};
+    return r;
+  };
+  auto common = [&](cta::CArgs& a, int l) {
+    memset(&a, 0, sizeof(a));
+    a.ct = tables(l);
+    a.nt = tables(l + 1);
+    a.cr = rec(l);
+    a.nr = rec(l + 1);
+    a.n = n;
+    a.mx = mx;
+    a.level = l;
+    a.ntracks = T_;
+    a.track_start = dtab + P.off_ts;
+    a.state = p->state;
+    a.cov = want_cov ? p->covariance : nullptr;
+    a.flag = dflag;
+    a.scratch = scratch;
+    a.scratch_per_cta = per_cta;
+  };
+  auto grid = [&](int64_t items) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(items, ncta)); };
+  {
+    cta::CArgs a;
+    common(a, 0);
+    a.ce = eq_level(0);
+    const cta::RawA raw{p->H, p->F, p->c, p->K, p->G, p->o, p->C, p->K_type, p->C_type, p->obs_rows, p->mmax};
+    UKG_LAUNCH(UKG_K_WEIGH, st, (cta::weigh_cta<<<grid(p->nsteps), cta::NT, 0, st>>>(a, raw, p->nsteps)));
+  }
+  for (int l = 0; l < nlev; ++l) {
+    cta::CArgs a;
+    common(a, l);
+    a.ce = eq_level(l);
+    if (l + 1 < nlev) a.ne = eq_level(l + 1);
+    if (lp[l].npairs > 0) UKG_LAUNCH(UKG_K_PAIR, st, (cta::pair_cta<<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
+    if (lp[l].ntail > 0) UKG_LAUNCH(UKG_K_TAIL, st, (cta::tail_cta<<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
+  }
+  for (int l = nlev - 2; l >= 0; --l) {
+    cta::CArgs a;
+    common(a, l);
+    if (lp[l].nsolve > 0)
+      UKG_LAUNCH(UKG_K_SOLVE, st,
+                 (cta::solve_cta<<<grid(lp[l].nsolve), cta::NT, 0, st>>>(a, want_cov ? 1 : 0)));
+  }
+  int hflag = 0;
+  cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return ukg_set_error(KALMAN_GPU_ECUDA, "odd-even smoother: %s", cudaGetErrorString(e));
+  ukg_prof_collect();
+  if (hflag & 4) return ukg_set_error(KALMAN_GPU_EINVAL, "malformed input: observation rows outside [0, mmax] or an "
+                                     "unknown covariance type");
+  if (hflag & 1) return ukg_set_error(KALMAN_GPU_ESINGULAR, "a covariance factor is not positive definite");
+  if (hflag & 2) return ukg_set_error(KALMAN_GPU_ESINGULAR, "zero pivot: the smoothing problem is not observable");
+  return 0;
+}
+
 extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream)
 {
   if (p->nsteps == 0) return 0;
   const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
+  const int mxp = p->mmax > p->n ? p->mmax : p->n;
+  if (p->n >= kCtaMinN || mxp > 8) { /* larger shapes: CTA kernels, FP64 (also for FP32_REFINE requests) */
+    if (mxp > kCtaMaxN)
+      return ukg_set_error(KALMAN_GPU_EINVAL, "state dimension %d (observation rows %d) above this build's limit %d",
+                           p->n, p->mmax, kCtaMaxN);
+    Plan P;
+    const size_t need = build_plan(p, want_cov, false, false, P, nullptr, 0);
+    if (need == 0) return ukg_set_error(KALMAN_GPU_EINVAL, "tracks longer than 2^%d steps", kMaxLevels - 1);
+    if (int e = ensure_mapped_tables(need)) return e;
+    build_plan(p, want_cov, false, false, P, tl_mtab.host, need);
+    const int ncta = cta_count();
+    const int64_t per = cta_scratch_per_cta(p->n, p->mmax);
+    const size_t scratch_off = align_up(P.bytes, 256);
+    void* base = nullptr;
+    if (int e = ensure_workspace(scratch_off + (size_t)ncta * per * sizeof(double), &base)) return e;
+    return run_plan_cta(options, p, (cudaStream_t)cuda_stream, P, tl_mtab.dev, (char*)base,
+                        (double*)((char*)base + scratch_off), per, ncta);
+  }
   const bool fp32 = (options & KALMAN_GPU_FP32_REFINE) != 0;
   Plan P;
   const size_t need = build_plan(p, want_cov, fp32, fp32, P, nullptr, 0);

@@ -1,0 +1,624 @@
+/*
+ * oddeven_cta.cuh -- the odd-even smoother for larger state dimensions, one
+ * thread block (CTA) per work item.  Included by oddeven.cu (it uses that
+ * file's Tables, find_track and orig_step).
+ *
+ * The per-thread kernels of oddeven.cu give a whole step pair to one thread;
+ * past n = 8 a pair's panels (up to 2n x (3n+1) entries) no longer fit one
+ * thread's share of shared memory.  Here the CTA's threads share each item:
+ * every panel is a row-major matrix in a per-CTA region of global scratch
+ * (L1/L2 resident), each Householder reflector is built from a block-wide
+ * reduction and applied with one thread per column (consecutive threads touch
+ * consecutive addresses), triangular solves run one thread per right-hand
+ * side, and the grid is persistent (CTAs loop over the items).  Same algorithm
+ * and arithmetic as the per-thread kernels (c/kalman_oddeven_smoother.c):
+ *   weigh_cta  steps_weigh 1620-1659 + kalman_covariance_matrix_weigh
+ *   pair_cta   stages A (379-457), C (526-560), B (460-523) and renaming
+ *   tail_cta   the odd-length fix-up (1452-1476) and the base case (1360-1423)
+ *   solve_cta  Solve_Estimates 614-975 (states and the covariance recurrence)
+ * Level arrays are slot-major here (all entries of a slot contiguous).  FP64.
+ */
+#pragma once
+
+namespace cta {
+
+constexpr int NT = 128; /* threads per CTA; rows of a panel beyond NT are looped */
+
+/* slot-major view: entry e of slot s at p[s * w + e] */
+template <typename T>
+struct Aos {
+  T* p;
+  int64_t w;
+  __device__ __forceinline__ T& at(int e, int64_t s) const { return p[s * w + e]; }
+};
+template <typename T>
+struct EqA {
+  Aos<T> F, H, c, G, o;
+  int32_t* m;
+};
+template <typename T>
+struct RecA {
+  Aos<T> R, Ft, Y, rhs, U;
+};
+
+struct CArgs {
+  Tables ct, nt;
+  EqA<double> ce, ne;
+  RecA<double> cr, nr;
+  int n, mx, level, ntracks;
+  const int64_t* track_start;
+  double* state;
+  double* cov;
+  int* flag;
+  double* scratch; /* per CTA: scratch + blockIdx.x * scratch_per_cta */
+  int64_t scratch_per_cta;
+};
+
+struct RawA {
+  const double *H, *F, *c, *K, *G, *o, *C;
+  const char *K_type, *C_type;
+  const int32_t* obs_rows;
+  int mmax;
+};
+
+/* sum over the CTA, returned to every thread; red holds >= 33 doubles */
+__device__ __forceinline__ double block_sum(double v, double* red)
+{
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < NT / 32; ++w) s += red[w];
+    red[32] = s;
+  }
+  __syncthreads();
+  const double r = red[32];
+  __syncthreads(); /* red may be reused right away */
+  return r;
+}
+
+/* Householder QR of the row-major panel A (ld) on its first `rows` rows: the
+ * first npiv columns are triangularized (reflectors stored below the
+ * diagonal, LAPACK dlarfg convention), Q^T is applied to all `cols` columns. */
+__device__ void householder(double* A, int ld, int rows, int npiv, int cols, double* red)
+{
+  const int tid = threadIdx.x;
+  const int kmax = rows < npiv ? rows : npiv;
+  for (int k = 0; k < kmax; ++k) {
+    double part = 0.0;
+    for (int i = k + 1 + tid; i < rows; i += NT) {
+      const double x = A[(int64_t)i * ld + k];
+      part = fma(x, x, part);
+    }
+    const double tail = block_sum(part, red);
+    const double alpha = A[(int64_t)k * ld + k];
+    if (tail == 0.0) continue; /* identity reflector: every thread agrees */
+    const double beta = -copysign(sqrt(fma(alpha, alpha, tail)), alpha);
+    const double amb = alpha - beta;
+    const double inv = 1.0 / (beta * amb);
+    const double t = -(amb * amb) * inv, scale = beta * inv;
+    for (int i = k + 1 + tid; i < rows; i += NT) A[(int64_t)i * ld + k] *= scale;
+    __syncthreads();
+    for (int j = k + 1 + tid; j < cols; j += NT) {
+      double d = A[(int64_t)k * ld + j];
+      for (int i = k + 1; i < rows; ++i) d = fma(A[(int64_t)i * ld + k], A[(int64_t)i * ld + j], d);
+      d *= t;
+      A[(int64_t)k * ld + j] -= d;
+      for (int i = k + 1; i < rows; ++i) A[(int64_t)i * ld + j] = fma(-d, A[(int64_t)i * ld + k], A[(int64_t)i * ld + j]);
+    }
+    if (tid == 0) A[(int64_t)k * ld + k] = beta;
+    __syncthreads();
+  }
+}
+
+/* x <- R^{-1} x for every column c0 <= c < c1 of the row-major X (ldx), R the
+ * upper triangle of the row-major Rm (ldr), n x n: one thread per column */
+__device__ void solve_upper_cols(const double* Rm, int ldr, int n, double* X, int ldx, int c0, int c1)
+{
+  for (int c = c0 + threadIdx.x; c < c1; c += NT)
+    for (int i = n - 1; i >= 0; --i) {
+      double s = X[(int64_t)i * ldx + c];
+      for (int k = i + 1; k < n; ++k) s = fma(-Rm[(int64_t)i * ldr + k], X[(int64_t)k * ldx + c], s);
+      X[(int64_t)i * ldx + c] = s / Rm[(int64_t)i * ldr + i];
+    }
+  __syncthreads();
+}
+
+/* x <- R^{-1} x for one vector x (n entries, shared by the CTA) */
+__device__ void solve_upper_vec(const double* Rm, int ldr, int n, double* x)
+{
+  for (int i = n - 1; i >= 0; --i) {
+    if (threadIdx.x == 0) x[i] /= Rm[(int64_t)i * ldr + i];
+    __syncthreads();
+    const double xi = x[i];
+    for (int k = threadIdx.x; k < i; k += NT) x[k] = fma(-Rm[(int64_t)k * ldr + i], xi, x[k]);
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ bool valid_cov_type(char t) { return t == 'W' || t == 'w' || t == 'C' || t == 'U' || t == 'F'; }
+
+/* Weighs the row-major panel B (rows x cols, ldb) by the covariance factor
+ * (cov column-major rows x rows, ld ldc, type): 'W' B <- W B, 'w' B <- diag B,
+ * 'C' B <- chol(cov)^{-1} B, 'U'/'F' B <- tril(cov)^{-1} B.  L (rows x rows
+ * row-major, ld rows) is scratch.  Returns false (in every thread) for a
+ * factor that is not positive definite or has a zero pivot. */
+__device__ bool weigh_panel(char type, const double* cov, int ldc, int rows, double* B, int ldb, int cols, double* L,
+                            double* red, double* tmp)
+{
+  const int tid = threadIdx.x;
+  if (type == 'w') {
+    for (int e = tid; e < rows * cols; e += NT) {
+      const int i = e / cols, c = e - i * cols;
+      B[(int64_t)i * ldb + c] *= cov[i];
+    }
+    __syncthreads();
+    return true;
+  }
+  if (type == 'W') { /* B <- W B, one thread per column, W read from the caller's array */
+    for (int c = tid; c < cols; c += NT) {
+      for (int i = 0; i < rows; ++i) {
+        double s = 0.0;
+        for (int j = 0; j < rows; ++j) s = fma(cov[(int64_t)j * ldc + i], B[(int64_t)j * ldb + c], s);
+        tmp[(int64_t)i * NT + tid] = s;
+      }
+      for (int i = 0; i < rows; ++i) B[(int64_t)i * ldb + c] = tmp[(int64_t)i * NT + tid];
+    }
+    __syncthreads();
+    return true;
+  }
+  if (type != 'C' && type != 'U' && type != 'F') return true;
+  for (int e = tid; e < rows * rows; e += NT) {
+    const int i = e / rows, j = e - i * rows;
+    L[e] = i >= j ? cov[(int64_t)j * ldc + i] : 0.0;
+  }
+  __syncthreads();
+  __shared__ int bad_s;
+  if (tid == 0) bad_s = 0;
+  __syncthreads();
+  if (type == 'C') { /* right-looking Cholesky, in place in L */
+    for (int j = 0; j < rows; ++j) {
+      if (tid == 0) {
+        const double d = L[(int64_t)j * rows + j];
+        if (!(d > 0.0)) bad_s = 1;
+        L[(int64_t)j * rows + j] = d > 0.0 ? sqrt(d) : 1.0;
+      }
+      __syncthreads();
+      const double ljj = L[(int64_t)j * rows + j];
+      for (int i = j + 1 + tid; i < rows; i += NT) L[(int64_t)i * rows + j] /= ljj;
+      __syncthreads();
+      for (int i = j + 1 + tid; i < rows; i += NT) {
+        const double lij = L[(int64_t)i * rows + j];
+        for (int l = j + 1; l <= i; ++l) L[(int64_t)i * rows + l] = fma(-lij, L[(int64_t)l * rows + j], L[(int64_t)i * rows + l]);
+      }
+      __syncthreads();
+    }
+  } else {
+    if (tid == 0)
+      for (int j = 0; j < rows; ++j)
+        if (L[(int64_t)j * rows + j] == 0.0) bad_s = 1;
+    __syncthreads();
+  }
+  /* forward substitution, one thread per column */
+  for (int c = tid; c < cols; c += NT)
+    for (int i = 0; i < rows; ++i) {
+      double s = B[(int64_t)i * ldb + c];
+      for (int k = 0; k < i; ++k) s = fma(-L[(int64_t)i * rows + k], B[(int64_t)k * ldb + c], s);
+      B[(int64_t)i * ldb + c] = s / L[(int64_t)i * rows + i];
+    }
+  __syncthreads();
+  const bool ok = bad_s == 0;
+  __syncthreads();
+  return ok;
+}
+
+/* ---------------------------------------------------------------------------
+ * level 0: weighing.  Per step: panel [H | -F | c] (n x (2n+1)) weighed by K's
+ * factor, panel [G | o] (m x (n+1)) by C's; written slot-major to level 0.
+ * Scratch: n^2 (L) + n (2n+1) (panel) + rows x NT (the 'W' product).
+ * ------------------------------------------------------------------------ */
+__global__ void __launch_bounds__(NT) weigh_cta(CArgs a, RawA raw, int64_t nsteps)
+{
+  __shared__ double red[33];
+  const int n = a.n, mx = a.mx, mm = raw.mmax, tid = threadIdx.x;
+  const int rmax = n > mm ? n : mm;
+  double* L = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
+  double* B = L + (int64_t)rmax * rmax;
+  double* tmp = B + (int64_t)rmax * (2 * n + 1);
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t g = blockIdx.x; g < nsteps; g += gridDim.x) {
+    const int t = find_track(a.track_start, a.ntracks, g);
+    const int64_t i = g - a.track_start[t], q = a.ct.slot[t] + i;
+    bool bad = false;
+    if (i > 0) {
+      const int ld = 2 * n + 1;
+      for (int e = tid; e < n * ld; e += NT) {
+        const int r = e / ld, c = e - r * ld;
+        double v;
+        if (c < n) v = raw.H[g * nn + (int64_t)c * n + r];
+        else if (c < 2 * n) v = -raw.F[g * nn + (int64_t)(c - n) * n + r];
+        else v = raw.c[g * n + r];
+        B[e] = v;
+      }
+      __syncthreads();
+      const char kt = raw.K_type[g];
+      if (tid == 0 && !valid_cov_type(kt)) atomicOr(a.flag, 4);
+      bad |= !weigh_panel(kt, raw.K + g * nn, n, n, B, ld, ld, L, red, tmp);
+      for (int e = tid; e < n * ld; e += NT) {
+        const int r = e / ld, c = e - r * ld;
+        if (c < n) a.ce.H.at(c * n + r, q) = B[e];
+        else if (c < 2 * n) a.ce.F.at((c - n) * n + r, q) = B[e];
+        else a.ce.c.at(r, q) = B[e];
+      }
+      __syncthreads();
+    }
+    int m = raw.obs_rows[g];
+    if (m < 0 || m > mm) {
+      m = 0;
+      if (tid == 0) atomicOr(a.flag, 4);
+    }
+    if (tid == 0) a.ce.m[q] = m;
+    if (m > 0) {
+      const int ld = n + 1;
+      for (int e = tid; e < m * ld; e += NT) {
+        const int r = e / ld, c = e - r * ld;
+        B[e] = c < n ? raw.G[g * (int64_t)mm * n + (int64_t)c * mm + r] : raw.o[g * mm + r];
+      }
+      __syncthreads();
+      const char ct = raw.C_type[g];
+      if (tid == 0 && !valid_cov_type(ct)) atomicOr(a.flag, 4);
+      bad |= !weigh_panel(ct, raw.C + g * (int64_t)mm * mm, mm, m, B, ld, ld, L, red, tmp);
+      for (int e = tid; e < m * ld; e += NT) {
+        const int r = e / ld, c = e - r * ld;
+        if (c < n) a.ce.G.at(c * mx + r, q) = B[e];
+        else a.ce.o.at(r, q) = B[e];
+      }
+      __syncthreads();
+    }
+    if (bad && tid == 0) atomicOr(a.flag, 1);
+  }
+}
+
+/* ---------------------------------------------------------------------------
+ * forward elimination of one pair per CTA: stages A, C, B
+ * Scratch: the largest panel, 2n x (3n+1).
+ * ------------------------------------------------------------------------ */
+__global__ void __launch_bounds__(NT) pair_cta(CArgs a)
+{
+  __shared__ double red[33];
+  const int n = a.n, mx = a.mx, tid = threadIdx.x;
+  double* A = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
+  const EqA<double>& C = a.ce;
+  const EqA<double>& Nx = a.ne;
+  const RecA<double>& Rr = a.cr;
+  for (int64_t item = blockIdx.x; item < a.ct.npairs; item += gridDim.x) {
+    const int t = find_track(a.ct.pair, a.ntracks, item);
+    const int64_t p = item - a.ct.pair[t];
+    const int64_t sj = a.ct.slot[t] + 2 * p, sj1 = sj + 1;
+    const int64_t sn = a.nt.slot[t] + p, se = a.ct.solve[t] + p;
+    const int mj = C.m[sj], mj1 = C.m[sj1];
+
+    /* stage A: [G_j | o_j | 0; F_{j+1} | c_{j+1} | H_{j+1}], n pivots */
+    {
+      const int rows = mj + n, ld = 2 * n + 1;
+      for (int e = tid; e < rows * ld; e += NT) {
+        const int r = e / ld, c = e - r * ld;
+        double v;
+        if (r < mj) v = c < n ? C.G.at(c * mx + r, sj) : c == n ? C.o.at(r, sj) : 0.0;
+        else {
+          const int rr = r - mj;
+          v = c < n ? C.F.at(c * n + rr, sj1) : c == n ? C.c.at(rr, sj1) : C.H.at((c - n - 1) * n + rr, sj1);
+        }
+        A[e] = v;
+      }
+      __syncthreads();
+      householder(A, ld, rows, n, ld, red);
+      for (int e = tid; e < n * n; e += NT) {
+        const int r = e / n, c = e - r * n; /* R~ (r, c), Y~ (r, c) */
+        Rr.R.at(c * n + r, se) = r <= c ? A[(int64_t)r * ld + c] : 0.0;
+        Rr.Y.at(c * n + r, se) = A[(int64_t)r * ld + n + 1 + c];
+      }
+      for (int r = tid; r < n; r += NT) Rr.rhs.at(r, se) = A[(int64_t)r * ld + n];
+      for (int e = tid; e < mj * n; e += NT) { /* H~ and o~: the next level's first observation rows */
+        const int r = e / n, c = e - r * n;
+        Nx.G.at(c * mx + r, sn) = A[(int64_t)(n + r) * ld + n + 1 + c];
+      }
+      for (int r = tid; r < mj; r += NT) Nx.o.at(r, sn) = A[(int64_t)(n + r) * ld + n];
+      __syncthreads();
+    }
+    /* stage C: [H~ | o~; G_{j+1} | o_{j+1}] */
+    if (mj + mj1 == 0) {
+      if (tid == 0) Nx.m[sn] = 0;
+    } else {
+      const int rows = mj + mj1, ld = n + 1;
+      for (int e = tid; e < rows * ld; e += NT) {
+        const int r = e / ld, c = e - r * ld;
+        A[e] = r < mj ? (c < n ? Nx.G.at(c * mx + r, sn) : Nx.o.at(r, sn))
+                      : (c < n ? C.G.at(c * mx + (r - mj), sj1) : C.o.at(r - mj, sj1));
+      }
+      __syncthreads();
+      householder(A, ld, rows, n, ld, red);
+      const int g2 = rows < n ? rows : n;
+      for (int e = tid; e < g2 * n; e += NT) {
+        const int r = e / n, c = e - r * n;
+        Nx.G.at(c * mx + r, sn) = r <= c ? A[(int64_t)r * ld + c] : 0.0;
+      }
+      for (int r = tid; r < g2; r += NT) Nx.o.at(r, sn) = A[(int64_t)r * ld + n];
+      if (tid == 0) Nx.m[sn] = g2;
+      __syncthreads();
+    }
+    /* stage B: [H_j | F_j | c_j | 0; R~ | 0 | rhs~ | Y~] */
+    if (p == 0) {
+      for (int e = tid; e < n * n; e += NT) Rr.Ft.at(e, se) = 0.0;
+      __syncthreads();
+      continue;
+    }
+    {
+      const int rows = 2 * n, ld = 3 * n + 1;
+      for (int e = tid; e < rows * ld; e += NT) {
+        const int r = e / ld, c = e - r * ld;
+        double v;
+        if (r < n) {
+          v = c < n ? C.H.at(c * n + r, sj) : c < 2 * n ? C.F.at((c - n) * n + r, sj) : c == 2 * n ? C.c.at(r, sj) : 0.0;
+        } else {
+          const int rr = r - n;
+          v = c < n ? (rr <= c ? Rr.R.at(c * n + rr, se) : 0.0)
+              : c < 2 * n ? 0.0 : c == 2 * n ? Rr.rhs.at(rr, se) : Rr.Y.at((c - 2 * n - 1) * n + rr, se);
+        }
+        A[e] = v;
+      }
+      __syncthreads();
+      householder(A, ld, rows, n, ld, red);
+      for (int e = tid; e < n * n; e += NT) {
+        const int r = e / n, c = e - r * n;
+        Rr.R.at(c * n + r, se) = r <= c ? A[(int64_t)r * ld + c] : 0.0;
+        Rr.Ft.at(c * n + r, se) = A[(int64_t)r * ld + n + c];
+        Nx.F.at(c * n + r, sn) = A[(int64_t)(n + r) * ld + n + c];
+        Rr.Y.at(c * n + r, se) = A[(int64_t)r * ld + 2 * n + 1 + c];
+        Nx.H.at(c * n + r, sn) = A[(int64_t)(n + r) * ld + 2 * n + 1 + c];
+      }
+      for (int r = tid; r < n; r += NT) {
+        Rr.rhs.at(r, se) = A[(int64_t)r * ld + 2 * n];
+        Nx.c.at(r, sn) = A[(int64_t)(n + r) * ld + 2 * n];
+      }
+      __syncthreads();
+    }
+  }
+}
+
+/* ---------------------------------------------------------------------------
+ * odd-length tracks: the single last step and its fix-up, or the base case.
+ * Scratch: the (n+m) x (2n+1) panel, an n x n inverse, an n-vector.
+ * ------------------------------------------------------------------------ */
+__global__ void __launch_bounds__(NT) tail_cta(CArgs a)
+{
+  __shared__ double red[33];
+  const int n = a.n, mx = a.mx, tid = threadIdx.x;
+  double* A = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
+  const EqA<double>& C = a.ce;
+  const EqA<double>& Nx = a.ne;
+  const RecA<double>& Rr = a.cr;
+  for (int64_t item = blockIdx.x; item < a.ct.ntail; item += gridDim.x) {
+    const int t = (int)a.ct.tail[item];
+    const int64_t L = a.ct.L[t], sb = a.ct.slot[t];
+    if (L == 1) { /* base case: x = R^{-1} Q^T o, S = R^{-1} R^{-T} */
+      const int m0 = C.m[sb];
+      const int64_t os = orig_step(a.track_start, a.level, t, 0);
+      double* x = a.state + os * n;
+      double* S = a.cov ? a.cov + os * (int64_t)n * n : nullptr;
+      if (m0 < n) {
+        for (int i = tid; i < n; i += NT) x[i] = NAN;
+        if (S)
+          for (int e = tid; e < n * n; e += NT) S[e] = NAN;
+        if (tid == 0) atomicOr(a.flag, 2);
+        __syncthreads();
+        continue;
+      }
+      const int ld = n + 1;
+      for (int e = tid; e < m0 * ld; e += NT) {
+        const int r = e / ld, c = e - r * ld;
+        A[e] = c < n ? C.G.at(c * mx + r, sb) : C.o.at(r, sb);
+      }
+      __syncthreads();
+      householder(A, ld, m0, n, ld, red);
+      if (tid == 0)
+        for (int i = 0; i < n; ++i)
+          if (A[(int64_t)i * ld + i] == 0.0) atomicOr(a.flag, 2);
+      double* v = A + (int64_t)m0 * ld; /* the right-hand side, then x */
+      for (int i = tid; i < n; i += NT) v[i] = A[(int64_t)i * ld + n];
+      __syncthreads();
+      solve_upper_vec(A, ld, n, v);
+      for (int i = tid; i < n; i += NT) x[i] = v[i];
+      if (S) {
+        double* Ri = v + n; /* R^{-1}, row-major n x n */
+        for (int e = tid; e < n * n; e += NT) Ri[e] = (e / n == e % n) ? 1.0 : 0.0;
+        __syncthreads();
+        solve_upper_cols(A, ld, n, Ri, n, 0, n);
+        for (int e = tid; e < n * n; e += NT) { /* S(r, c) = sum_k Ri(r, k) Ri(c, k) */
+          const int r = e / n, c = e - r * n;
+          double s = 0.0;
+          for (int k = (r > c ? r : c); k < n; ++k) s = fma(Ri[(int64_t)r * n + k], Ri[(int64_t)c * n + k], s);
+          S[(int64_t)c * n + r] = s;
+        }
+      }
+      __syncthreads();
+      continue;
+    }
+    /* single last step s = L-1 of an odd-length level */
+    const int64_t s = sb + L - 1;
+    const int64_t es = a.ct.solve[t] + (L - 1) / 2;
+    const int64_t sn = a.nt.slot[t] + L / 2 - 1;
+    const int ms = C.m[s], mt = ms < n ? ms : n;
+    /* stage A on [G_s | o_s]: its R~ and o' go into the lower rows of the
+       stage-B panel, built in the same scratch below it */
+    const int ldA = n + 1, ldT = 2 * n + 1, rowsT = n + mt;
+    double* WS = A;
+    double* WT = A + (int64_t)(ms > 0 ? ms : 1) * ldA;
+    if (ms > 0) {
+      for (int e = tid; e < ms * ldA; e += NT) {
+        const int r = e / ldA, c = e - r * ldA;
+        WS[e] = c < n ? C.G.at(c * mx + r, s) : C.o.at(r, s);
+      }
+      __syncthreads();
+      householder(WS, ldA, ms, n, ldA, red);
+    }
+    for (int e = tid; e < rowsT * ldT; e += NT) {
+      const int r = e / ldT, c = e - r * ldT;
+      double v;
+      if (r < n) v = c < n ? C.H.at(c * n + r, s) : c < 2 * n ? C.F.at((c - n) * n + r, s) : C.c.at(r, s);
+      else {
+        const int rr = r - n;
+        v = c < n ? (rr <= c ? WS[(int64_t)rr * ldA + c] : 0.0) : c < 2 * n ? 0.0 : WS[(int64_t)rr * ldA + n];
+      }
+      WT[e] = v;
+    }
+    __syncthreads();
+    householder(WT, ldT, rowsT, n, ldT, red);
+    for (int e = tid; e < n * n; e += NT) {
+      const int r = e / n, c = e - r * n;
+      Rr.R.at(c * n + r, es) = r <= c ? WT[(int64_t)r * ldT + c] : 0.0;
+      Rr.Ft.at(c * n + r, es) = WT[(int64_t)r * ldT + n + c];
+      Rr.Y.at(c * n + r, es) = 0.0;
+    }
+    for (int r = tid; r < n; r += NT) Rr.rhs.at(r, es) = WT[(int64_t)r * ldT + 2 * n];
+    __syncthreads();
+    /* fix-up: QR of [G~ o (gp rows of the next level's slot); Z o''] */
+    const int gp = Nx.m[sn], rF = gp + mt;
+    if (rF == 0) {
+      if (tid == 0) Nx.m[sn] = 0;
+      __syncthreads();
+      continue;
+    }
+    double* WF = WT + (int64_t)rowsT * ldT;
+    const int ldF = n + 1;
+    for (int e = tid; e < rF * ldF; e += NT) {
+      const int r = e / ldF, c = e - r * ldF;
+      WF[e] = r < gp ? (c < n ? Nx.G.at(c * mx + r, sn) : Nx.o.at(r, sn))
+                     : (c < n ? WT[(int64_t)(n + r - gp) * ldT + n + c] : WT[(int64_t)(n + r - gp) * ldT + 2 * n]);
+    }
+    __syncthreads();
+    householder(WF, ldF, rF, n, ldF, red);
+    const int g2 = rF < n ? rF : n;
+    for (int e = tid; e < g2 * n; e += NT) {
+      const int r = e / n, c = e - r * n;
+      Nx.G.at(c * mx + r, sn) = r <= c ? WF[(int64_t)r * ldF + c] : 0.0;
+    }
+    for (int r = tid; r < g2; r += NT) Nx.o.at(r, sn) = WF[(int64_t)r * ldF + n];
+    if (tid == 0) Nx.m[sn] = g2;
+    __syncthreads();
+  }
+}
+
+/* ---------------------------------------------------------------------------
+ * back-substitution and covariance recurrence of one even step per CTA:
+ *   x_j = R^{-1}(rhs - Ft x_{j-1} - Y x_{j+1})
+ *   W = B Sigma (B = [Ft Y], Sigma the joint covariance of x_{j-1}, x_{j+1})
+ *   cov(x_j, x_{j-1}) = -R^{-1} W[:, 0:n], cov(x_j, x_{j+1}) = -R^{-1} W[:, n:2n]
+ *   S_j = R^{-1} (I + W B^T) R^{-T}
+ * Scratch (row-major): R, B (n x 2n), W (n x 2n), M, X (n x n each), x.
+ * ------------------------------------------------------------------------ */
+__global__ void __launch_bounds__(NT) solve_cta(CArgs a, int want_cov)
+{
+  const int n = a.n, tid = threadIdx.x;
+  const int64_t nn = (int64_t)n * n;
+  double* R = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
+  double* Bm = R + nn;       /* n x 2n */
+  double* W = Bm + 2 * nn;   /* n x 2n */
+  double* M = W + 2 * nn;    /* n x n */
+  double* X = M + nn;        /* n x n */
+  double* xv = X + nn;       /* n */
+  const RecA<double>& Rr = a.cr;
+  for (int64_t item = blockIdx.x; item < a.ct.nsolve; item += gridDim.x) {
+    const int t = find_track(a.ct.solve, a.ntracks, item);
+    const int64_t j = 2 * (item - a.ct.solve[t]), L = a.ct.L[t];
+    const bool hp = j > 0, hn = j + 1 < L;
+    const int64_t oj = orig_step(a.track_start, a.level, t, j);
+    const int64_t om = hp ? orig_step(a.track_start, a.level, t, j - 1) : 0;
+    const int64_t op = hn ? orig_step(a.track_start, a.level, t, j + 1) : 0;
+    for (int e = tid; e < n * n; e += NT) {
+      const int r = e / n, c = e - r * n;
+      R[e] = Rr.R.at(c * n + r, item);
+      Bm[(int64_t)r * 2 * n + c] = hp ? Rr.Ft.at(c * n + r, item) : 0.0;
+      Bm[(int64_t)r * 2 * n + n + c] = hn ? Rr.Y.at(c * n + r, item) : 0.0;
+    }
+    __syncthreads();
+    /* state */
+    for (int r = tid; r < n; r += NT) {
+      double s = Rr.rhs.at(r, item);
+      if (hp)
+        for (int k = 0; k < n; ++k) s = fma(-Bm[(int64_t)r * 2 * n + k], a.state[om * n + k], s);
+      if (hn)
+        for (int k = 0; k < n; ++k) s = fma(-Bm[(int64_t)r * 2 * n + n + k], a.state[op * n + k], s);
+      xv[r] = s;
+    }
+    __syncthreads();
+    solve_upper_vec(R, n, n, xv);
+    for (int r = tid; r < n; r += NT) a.state[oj * n + r] = xv[r];
+    if (tid == 0)
+      for (int i = 0; i < n; ++i)
+        if (R[(int64_t)i * n + i] == 0.0) atomicOr(a.flag, 2);
+    if (!want_cov) {
+      __syncthreads();
+      continue;
+    }
+    /* W = B Sigma, one thread per row of W; Sigma entries are shared reads */
+    const double* Smm = hp ? a.cov + om * nn : nullptr;
+    const double* Spp = hn ? a.cov + op * nn : nullptr;
+    const int64_t smp = (hp && hn) ? a.nt.slot[t] + (j + 1) / 2 : 0;
+    auto sigma = [&](int k, int q) -> double { /* Sigma(k, q), 0 <= k, q < 2n */
+      if (k < n) {
+        if (q < n) return hp ? Smm[(int64_t)q * n + k] : 0.0;
+        return (hp && hn) ? a.nr.U.at((q - n) * n + k, smp) : 0.0; /* Smp(k, q-n) */
+      }
+      if (q < n) return (hp && hn) ? a.nr.U.at((k - n) * n + q, smp) : 0.0; /* Smp(q, k-n) */
+      return hn ? Spp[(int64_t)(q - n) * n + (k - n)] : 0.0;
+    };
+    const int k0 = hp ? 0 : n, k1 = hn ? 2 * n : n;
+    for (int r = tid; r < n; r += NT)
+      for (int q = k0; q < k1; ++q) {
+        double s = 0.0;
+        for (int k = k0; k < k1; ++k) s = fma(Bm[(int64_t)r * 2 * n + k], sigma(k, q), s);
+        W[(int64_t)r * 2 * n + q] = s;
+      }
+    for (int r = tid; r < n; r += NT)
+      for (int q = 0; q < 2 * n; ++q)
+        if (q < k0 || q >= k1) W[(int64_t)r * 2 * n + q] = 0.0;
+    __syncthreads();
+    /* M = I + W B^T */
+    for (int e = tid; e < n * n; e += NT) {
+      const int r = e / n, c = e - r * n;
+      double s = r == c ? 1.0 : 0.0;
+      for (int q = k0; q < k1; ++q) s = fma(W[(int64_t)r * 2 * n + q], Bm[(int64_t)c * 2 * n + q], s);
+      M[e] = s;
+    }
+    __syncthreads();
+    if (a.level > 0) { /* off-diagonal blocks: -R^{-1} W */
+      solve_upper_cols(R, n, n, W, 2 * n, k0, k1);
+      for (int e = tid; e < n * 2 * n; e += NT) {
+        const int r = e / (2 * n), q = e - r * 2 * n;
+        if (q < k0 || q >= k1) continue;
+        if (q < n) Rr.U.at(r * n + q, a.ct.slot[t] + j) = -W[e];          /* cov(x_{j-1}, x_j)(q, r) */
+        else Rr.U.at((q - n) * n + r, a.ct.slot[t] + j + 1) = -W[e];      /* cov(x_j, x_{j+1})(r, q-n) */
+      }
+      __syncthreads();
+    }
+    /* S = R^{-1} M R^{-T}: X = R^{-1} M, then S^T = R^{-1} X^T */
+    solve_upper_cols(R, n, n, M, n, 0, n);
+    for (int e = tid; e < n * n; e += NT) {
+      const int r = e / n, c = e - r * n;
+      X[(int64_t)c * n + r] = M[e];
+    }
+    __syncthreads();
+    solve_upper_cols(R, n, n, X, n, 0, n);
+    double* So = a.cov + oj * nn;
+    for (int e = tid; e < n * n; e += NT) { /* X now holds S^T = S; column-major out */
+      const int r = e / n, c = e - r * n;
+      So[(int64_t)c * n + r] = X[e];
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace cta
