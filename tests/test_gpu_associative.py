@@ -89,3 +89,26 @@ def test_non_square_first_observation_is_rejected():
     with pytest.raises(native.KalmanError) as e:
         native.smooth(P, "associative")
     assert e.value.status == 1
+
+
+@pytest.mark.parametrize("n,k", [(9, 41), (12, 200), (24, 80), (48, 30)])
+def test_larger_states_cta_path(n, k):
+    """State dimensions past 8 run one thread block per element or combine:
+    parity with the oracle, with missing observations and short tracks."""
+    P = pb.random_dynamics([k, 37, 2], n, n // 2, seed=5 + n, per_step=True, missing=0.1)
+    X, S = native.smooth(P, algorithm="associative")
+    st, Xo, So = oracle.smooth(P, "associative", covariance=True)
+    assert st == 0
+    assert oracle.rel_err_states(X, Xo) < TOL
+    assert oracle.rel_err_covs(S, So) < TOL
+
+
+def test_config1_shape_n48_covariance_types():
+    """n = 48, m = 24 (the associative benchmark shape) with the 'W' and 'w'
+    covariance forms."""
+    P = pb.random_dynamics([33, 4], 48, 24, seed=77, per_step=True, K_type="W", C_type="w", missing=0.05)
+    X, S = native.smooth(P, algorithm="associative")
+    st, Xo, So = oracle.smooth(P, "associative", covariance=True)
+    assert st == 0
+    assert oracle.rel_err_states(X, Xo) < TOL
+    assert oracle.rel_err_covs(S, So) < TOL

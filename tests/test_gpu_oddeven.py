@@ -147,7 +147,7 @@ def test_larger_states_cta_path(n, k):
 def test_config4_shape_n128():
     """n = 128, m = 64 (the largest shape this build accepts), all covariance
     types of the reference in one problem."""
-    P = pb.random_dynamics([23, 6], 128, 64, seed=21, per_step=True, K_type="W", C_type="U")
+    P = pb.random_dynamics([23, 6], 128, 64, seed=21, per_step=True, K_type="W", C_type="F")
     X, S = native.smooth(P)
     check(P, X, S)
     X2, _ = native.smooth(P, covariance=False, fp32_refine=True)

@@ -36,6 +36,7 @@
 #include <vector>
 
 #include "profiling.h"
+#include "cta_linalg.cuh"
 #include "ukgpu_internal.h"
 
 namespace {
@@ -636,6 +637,8 @@ struct ScanLevel {
   int64_t nup, ndown;
 };
 
+#include "associative_cta.cuh"
+
 /* up-sweep: level d+1 element p = a_{2p} (x) a_{2p+1}, or a_{2p} alone */
 template <class El>
 __global__ void up_kernel(int n, int T, ScanLevel lv, ScanLevel nx, El cur, El nxt, int* flag)
@@ -877,6 +880,22 @@ void plan_scan(const std::vector<int64_t>& L0, ScanPlan& sp, std::vector<int64_t
   }
 }
 
+/* waits for the smoother's kernels and reports its flags */
+int finish(cudaStream_t st, int* dflag)
+{
+  int hflag = 0;
+  cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return ukg_set_error(KALMAN_GPU_ECUDA, "associative smoother: %s", cudaGetErrorString(e));
+  ukg_prof_collect();
+  if (hflag & 4) return ukg_set_error(KALMAN_GPU_EINVAL, "malformed input: the associative smoother needs a square "
+                                     "observation at the first step of every track, observation rows within "
+                                     "[0, mmax] and known covariance types");
+  if (hflag & 2) return ukg_set_error(KALMAN_GPU_ESINGULAR, "a singular matrix in the associative smoother");
+  return 0;
+}
+
 }  // namespace
 
 extern "C" void ukg_release_associative_workspace(void)
@@ -921,6 +940,25 @@ extern "C" int ukg_associative_device(uint32_t options, const kalman_gpu_problem
   bytes = lev_base;
   for (int l = 0; l < sp.nlev; ++l) o_sl[l] = take((size_t)std::max<int64_t>(sp.cap[l], 1) * (2 * nn + n) * 8);
   bytes = std::max(bytes, f_end);
+  /* larger shapes run the CTA kernels, which need per-CTA scratch */
+  const bool cta_path = n >= 9 || mx > 8;
+  int ncta = 0;
+  int64_t per_cta = 0;
+  size_t o_scratch = 0;
+  if (cta_path) {
+    if (mx > 128)
+      return ukg_set_error(KALMAN_GPU_EINVAL, "state dimension %d (observation rows %d) above this build's limit 128",
+                           n, p->mmax);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    ncta = std::max(sms, 1) * 4;
+    const int64_t mxr = mx;
+    const int64_t elem = n + 2 * nn + mxr * 2 * n + mxr * (mxr + n + 1) + 2 * mxr * mxr + 2 * n * mxr + 2 * mxr +
+                         mxr * acta::NT;
+    per_cta = std::max(std::max(elem, 7 * nn + 4 * n), 7 * nn + n) + 32;
+    o_scratch = take((size_t)ncta * per_cta * sizeof(double));
+  }
   void* base = nullptr;
   if (int e = ensure(bytes, &base)) return e;
   char* B = (char*)base;
@@ -959,6 +997,71 @@ extern "C" int ukg_associative_device(uint32_t options, const kalman_gpu_problem
     v.ndown = s.ndown[l];
     return v;
   };
+
+  if (cta_path) { /* larger shapes: one CTA per element or combine */
+    auto fel = [&](int l) {
+      const int64_t c = std::max<int64_t>(fp.cap[l], 1);
+      double* d = (double*)(B + o_fl[l]);
+      acta::FEl e;
+      e.A = {d, nn};
+      e.Z = {d + nn * c, nn};
+      e.J = {d + 2 * nn * c, nn};
+      e.b = {d + 3 * nn * c, n};
+      e.e = {d + (3 * nn + n) * c, n};
+      return e;
+    };
+    auto sel = [&](int l) {
+      const int64_t c = std::max<int64_t>(sp.cap[l], 1);
+      double* d = (double*)(B + o_sl[l]);
+      acta::SEl e;
+      e.E = {d, nn};
+      e.L = {d + nn * c, nn};
+      e.g = {d + 2 * nn * c, n};
+      return e;
+    };
+    auto level = [&](const ScanPlan& s2, int l) {
+      ScanLevel v;
+      v.L = dtab + s2.off_L[l];
+      v.start = dtab + s2.off_start[l];
+      v.up_items = dtab + s2.off_up[l];
+      v.down_items = dtab + s2.off_down[l];
+      v.nup = s2.nup[l];
+      v.ndown = s2.ndown[l];
+      return v;
+    };
+    double* scratch = (double*)(B + o_scratch);
+    acta::AArgs a{n, T, dtab + off_ts, p->state, p->covariance, dflag, scratch, per_cta};
+    acta::RawS raw{p->F, p->c, p->K, p->G, p->o, p->C, p->K_type, p->C_type, p->obs_rows, p->mmax};
+    auto g = [&](int64_t items) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(items, ncta)); };
+    const int64_t* fstart0 = dtab + fp.off_start[0];
+    UKG_LAUNCH(UKG_K_AS_ELEMENT, st, (acta::element_cta<<<g(N), acta::NT, 0, st>>>(a, raw, fel(0), fstart0, N)));
+    for (int l = 0; l + 1 < fp.nlev; ++l)
+      if (fp.nup[l] > 0)
+        UKG_LAUNCH(UKG_K_AS_SCAN, st,
+                   (acta::up_cta<acta::FEl><<<g(fp.nup[l]), acta::NT, 0, st>>>(
+                       n, T, level(fp, l), level(fp, l + 1), fel(l), fel(l + 1), dflag, scratch, per_cta)));
+    for (int l = fp.nlev - 2; l >= 0; --l)
+      if (fp.ndown[l] > 0)
+        UKG_LAUNCH(UKG_K_AS_SCAN, st,
+                   (acta::down_cta<acta::FEl><<<g(fp.ndown[l]), acta::NT, 0, st>>>(
+                       n, T, level(fp, l), level(fp, l + 1), fel(l), fel(l + 1), dflag, scratch, per_cta)));
+    UKG_LAUNCH(UKG_K_AS_ELEMENT, st, (acta::filtered_out_cta<<<g(N), 128, 0, st>>>(a, fel(0), fstart0, N)));
+    const int64_t* sstart0 = dtab + sp.off_start[0];
+    UKG_LAUNCH(UKG_K_AS_SMOOTH, st,
+               (acta::smooth_element_cta<<<g(N), acta::NT, 0, st>>>(a, raw, sel(0), sstart0, N)));
+    for (int l = 0; l + 1 < sp.nlev; ++l)
+      if (sp.nup[l] > 0)
+        UKG_LAUNCH(UKG_K_AS_SCAN, st,
+                   (acta::up_cta<acta::SEl><<<g(sp.nup[l]), acta::NT, 0, st>>>(
+                       n, T, level(sp, l), level(sp, l + 1), sel(l), sel(l + 1), dflag, scratch, per_cta)));
+    for (int l = sp.nlev - 2; l >= 0; --l)
+      if (sp.ndown[l] > 0)
+        UKG_LAUNCH(UKG_K_AS_SCAN, st,
+                   (acta::down_cta<acta::SEl><<<g(sp.ndown[l]), acta::NT, 0, st>>>(
+                       n, T, level(sp, l), level(sp, l + 1), sel(l), sel(l + 1), dflag, scratch, per_cta)));
+    UKG_LAUNCH(UKG_K_AS_SMOOTH, st, (acta::smoothed_out_cta<<<g(N), 128, 0, st>>>(a, sel(0), sstart0, N)));
+    return finish(st, dflag);
+  }
 
   Args a;
   a.n = n;
@@ -1020,15 +1123,5 @@ extern "C" int ukg_associative_device(uint32_t options, const kalman_gpu_problem
                      n, T, level(sp, l), level(sp, l + 1), selems(l), selems(l + 1), dflag)));
   UKG_LAUNCH(UKG_K_AS_SMOOTH, st, (smoothed_out_kernel<<<grid(N, ew), ew, 0, st>>>(a, selems(0), sstart0, N)));
 
-  int hflag = 0;
-  cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaError_t e = cudaStreamSynchronize(st);
-  if (e == cudaSuccess) e = cudaGetLastError();
-  if (e != cudaSuccess) return ukg_set_error(KALMAN_GPU_ECUDA, "associative smoother: %s", cudaGetErrorString(e));
-  ukg_prof_collect();
-  if (hflag & 4) return ukg_set_error(KALMAN_GPU_EINVAL, "malformed input: the associative smoother needs a square "
-                                     "observation at the first step of every track, observation rows within "
-                                     "[0, mmax] and known covariance types");
-  if (hflag & 2) return ukg_set_error(KALMAN_GPU_ESINGULAR, "a singular matrix in the associative smoother");
-  return 0;
+  return finish(st, dflag);
 }

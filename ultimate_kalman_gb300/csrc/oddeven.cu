@@ -55,6 +55,7 @@
 #include <cuda_runtime.h>
 
 #include "df64.cuh"
+#include "cta_linalg.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -2908,7 +2909,7 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
   };
   auto eqa = [&](size_t off, size_t off_m, int64_t S) {
     double* e = (double*)(B + off);
-    cta::EqA<double> d;
+    ctak::EqA<double> d;
     d.F = {e, nn};
     d.H = {e + nn * S, nn};
     d.c = {e + 2 * nn * S, n};
@@ -2921,7 +2922,7 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
     return (l & 1) ? eqa(P.o_eqA, P.o_mA, P.S1) : eqa(P.o_eq0, P.o_m0, P.S0);
   };
   auto rec = [&](int l) {
-    cta::RecA<double> r;
+    ctak::RecA<double> r;
     memset(&r, 0, sizeof(r));
     if (l >= nlev) return r;
     const int64_t E = std::max<int64_t>(lp[l].E, 1);
@@ -2933,7 +2934,7 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
     if (want_cov && l > 0) r.U = {(double*)(B + P.o_U[l]), nn};
     return r;
   };
-  auto common = [&](cta::CArgs& a, int l) {
+  auto common = [&](ctak::CArgs& a, int l) {
     memset(&a, 0, sizeof(a));
     a.ct = tables(l);
     a.nt = tables(l + 1);
@@ -2952,26 +2953,26 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
   };
   auto grid = [&](int64_t items) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(items, ncta)); };
   {
-    cta::CArgs a;
+    ctak::CArgs a;
     common(a, 0);
     a.ce = eq_level(0);
-    const cta::RawA raw{p->H, p->F, p->c, p->K, p->G, p->o, p->C, p->K_type, p->C_type, p->obs_rows, p->mmax};
-    UKG_LAUNCH(UKG_K_WEIGH, st, (cta::weigh_cta<<<grid(p->nsteps), cta::NT, 0, st>>>(a, raw, p->nsteps)));
+    const ctak::RawA raw{p->H, p->F, p->c, p->K, p->G, p->o, p->C, p->K_type, p->C_type, p->obs_rows, p->mmax};
+    UKG_LAUNCH(UKG_K_WEIGH, st, (ctak::weigh_cta<<<grid(p->nsteps), cta::NT, 0, st>>>(a, raw, p->nsteps)));
   }
   for (int l = 0; l < nlev; ++l) {
-    cta::CArgs a;
+    ctak::CArgs a;
     common(a, l);
     a.ce = eq_level(l);
     if (l + 1 < nlev) a.ne = eq_level(l + 1);
-    if (lp[l].npairs > 0) UKG_LAUNCH(UKG_K_PAIR, st, (cta::pair_cta<<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
-    if (lp[l].ntail > 0) UKG_LAUNCH(UKG_K_TAIL, st, (cta::tail_cta<<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
+    if (lp[l].npairs > 0) UKG_LAUNCH(UKG_K_PAIR, st, (ctak::pair_cta<<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
+    if (lp[l].ntail > 0) UKG_LAUNCH(UKG_K_TAIL, st, (ctak::tail_cta<<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
   }
   for (int l = nlev - 2; l >= 0; --l) {
-    cta::CArgs a;
+    ctak::CArgs a;
     common(a, l);
     if (lp[l].nsolve > 0)
       UKG_LAUNCH(UKG_K_SOLVE, st,
-                 (cta::solve_cta<<<grid(lp[l].nsolve), cta::NT, 0, st>>>(a, want_cov ? 1 : 0)));
+                 (ctak::solve_cta<<<grid(lp[l].nsolve), cta::NT, 0, st>>>(a, want_cov ? 1 : 0)));
   }
   int hflag = 0;
   cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st);

@@ -19,18 +19,11 @@
  * Level arrays are slot-major here (all entries of a slot contiguous).  FP64.
  */
 #pragma once
+#include "cta_linalg.cuh"
 
-namespace cta {
+namespace ctak {
+using namespace ::cta;
 
-constexpr int NT = 128; /* threads per CTA; rows of a panel beyond NT are looped */
-
-/* slot-major view: entry e of slot s at p[s * w + e] */
-template <typename T>
-struct Aos {
-  T* p;
-  int64_t w;
-  __device__ __forceinline__ T& at(int e, int64_t s) const { return p[s * w + e]; }
-};
 template <typename T>
 struct EqA {
   Aos<T> F, H, c, G, o;
@@ -60,159 +53,6 @@ struct RawA {
   const int32_t* obs_rows;
   int mmax;
 };
-
-/* sum over the CTA, returned to every thread; red holds >= 33 doubles */
-__device__ __forceinline__ double block_sum(double v, double* red)
-{
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) red[warp] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int w = 0; w < NT / 32; ++w) s += red[w];
-    red[32] = s;
-  }
-  __syncthreads();
-  const double r = red[32];
-  __syncthreads(); /* red may be reused right away */
-  return r;
-}
-
-/* Householder QR of the row-major panel A (ld) on its first `rows` rows: the
- * first npiv columns are triangularized (reflectors stored below the
- * diagonal, LAPACK dlarfg convention), Q^T is applied to all `cols` columns. */
-__device__ void householder(double* A, int ld, int rows, int npiv, int cols, double* red)
-{
-  const int tid = threadIdx.x;
-  const int kmax = rows < npiv ? rows : npiv;
-  for (int k = 0; k < kmax; ++k) {
-    double part = 0.0;
-    for (int i = k + 1 + tid; i < rows; i += NT) {
-      const double x = A[(int64_t)i * ld + k];
-      part = fma(x, x, part);
-    }
-    const double tail = block_sum(part, red);
-    const double alpha = A[(int64_t)k * ld + k];
-    if (tail == 0.0) continue; /* identity reflector: every thread agrees */
-    const double beta = -copysign(sqrt(fma(alpha, alpha, tail)), alpha);
-    const double amb = alpha - beta;
-    const double inv = 1.0 / (beta * amb);
-    const double t = -(amb * amb) * inv, scale = beta * inv;
-    for (int i = k + 1 + tid; i < rows; i += NT) A[(int64_t)i * ld + k] *= scale;
-    __syncthreads();
-    for (int j = k + 1 + tid; j < cols; j += NT) {
-      double d = A[(int64_t)k * ld + j];
-      for (int i = k + 1; i < rows; ++i) d = fma(A[(int64_t)i * ld + k], A[(int64_t)i * ld + j], d);
-      d *= t;
-      A[(int64_t)k * ld + j] -= d;
-      for (int i = k + 1; i < rows; ++i) A[(int64_t)i * ld + j] = fma(-d, A[(int64_t)i * ld + k], A[(int64_t)i * ld + j]);
-    }
-    if (tid == 0) A[(int64_t)k * ld + k] = beta;
-    __syncthreads();
-  }
-}
-
-/* x <- R^{-1} x for every column c0 <= c < c1 of the row-major X (ldx), R the
- * upper triangle of the row-major Rm (ldr), n x n: one thread per column */
-__device__ void solve_upper_cols(const double* Rm, int ldr, int n, double* X, int ldx, int c0, int c1)
-{
-  for (int c = c0 + threadIdx.x; c < c1; c += NT)
-    for (int i = n - 1; i >= 0; --i) {
-      double s = X[(int64_t)i * ldx + c];
-      for (int k = i + 1; k < n; ++k) s = fma(-Rm[(int64_t)i * ldr + k], X[(int64_t)k * ldx + c], s);
-      X[(int64_t)i * ldx + c] = s / Rm[(int64_t)i * ldr + i];
-    }
-  __syncthreads();
-}
-
-/* x <- R^{-1} x for one vector x (n entries, shared by the CTA) */
-__device__ void solve_upper_vec(const double* Rm, int ldr, int n, double* x)
-{
-  for (int i = n - 1; i >= 0; --i) {
-    if (threadIdx.x == 0) x[i] /= Rm[(int64_t)i * ldr + i];
-    __syncthreads();
-    const double xi = x[i];
-    for (int k = threadIdx.x; k < i; k += NT) x[k] = fma(-Rm[(int64_t)k * ldr + i], xi, x[k]);
-    __syncthreads();
-  }
-}
-
-__device__ __forceinline__ bool valid_cov_type(char t) { return t == 'W' || t == 'w' || t == 'C' || t == 'U' || t == 'F'; }
-
-/* Weighs the row-major panel B (rows x cols, ldb) by the covariance factor
- * (cov column-major rows x rows, ld ldc, type): 'W' B <- W B, 'w' B <- diag B,
- * 'C' B <- chol(cov)^{-1} B, 'U'/'F' B <- tril(cov)^{-1} B.  L (rows x rows
- * row-major, ld rows) is scratch.  Returns false (in every thread) for a
- * factor that is not positive definite or has a zero pivot. */
-__device__ bool weigh_panel(char type, const double* cov, int ldc, int rows, double* B, int ldb, int cols, double* L,
-                            double* red, double* tmp)
-{
-  const int tid = threadIdx.x;
-  if (type == 'w') {
-    for (int e = tid; e < rows * cols; e += NT) {
-      const int i = e / cols, c = e - i * cols;
-      B[(int64_t)i * ldb + c] *= cov[i];
-    }
-    __syncthreads();
-    return true;
-  }
-  if (type == 'W') { /* B <- W B, one thread per column, W read from the caller's array */
-    for (int c = tid; c < cols; c += NT) {
-      for (int i = 0; i < rows; ++i) {
-        double s = 0.0;
-        for (int j = 0; j < rows; ++j) s = fma(cov[(int64_t)j * ldc + i], B[(int64_t)j * ldb + c], s);
-        tmp[(int64_t)i * NT + tid] = s;
-      }
-      for (int i = 0; i < rows; ++i) B[(int64_t)i * ldb + c] = tmp[(int64_t)i * NT + tid];
-    }
-    __syncthreads();
-    return true;
-  }
-  if (type != 'C' && type != 'U' && type != 'F') return true;
-  for (int e = tid; e < rows * rows; e += NT) {
-    const int i = e / rows, j = e - i * rows;
-    L[e] = i >= j ? cov[(int64_t)j * ldc + i] : 0.0;
-  }
-  __syncthreads();
-  __shared__ int bad_s;
-  if (tid == 0) bad_s = 0;
-  __syncthreads();
-  if (type == 'C') { /* right-looking Cholesky, in place in L */
-    for (int j = 0; j < rows; ++j) {
-      if (tid == 0) {
-        const double d = L[(int64_t)j * rows + j];
-        if (!(d > 0.0)) bad_s = 1;
-        L[(int64_t)j * rows + j] = d > 0.0 ? sqrt(d) : 1.0;
-      }
-      __syncthreads();
-      const double ljj = L[(int64_t)j * rows + j];
-      for (int i = j + 1 + tid; i < rows; i += NT) L[(int64_t)i * rows + j] /= ljj;
-      __syncthreads();
-      for (int i = j + 1 + tid; i < rows; i += NT) {
-        const double lij = L[(int64_t)i * rows + j];
-        for (int l = j + 1; l <= i; ++l) L[(int64_t)i * rows + l] = fma(-lij, L[(int64_t)l * rows + j], L[(int64_t)i * rows + l]);
-      }
-      __syncthreads();
-    }
-  } else {
-    if (tid == 0)
-      for (int j = 0; j < rows; ++j)
-        if (L[(int64_t)j * rows + j] == 0.0) bad_s = 1;
-    __syncthreads();
-  }
-  /* forward substitution, one thread per column */
-  for (int c = tid; c < cols; c += NT)
-    for (int i = 0; i < rows; ++i) {
-      double s = B[(int64_t)i * ldb + c];
-      for (int k = 0; k < i; ++k) s = fma(-L[(int64_t)i * rows + k], B[(int64_t)k * ldb + c], s);
-      B[(int64_t)i * ldb + c] = s / L[(int64_t)i * rows + i];
-    }
-  __syncthreads();
-  const bool ok = bad_s == 0;
-  __syncthreads();
-  return ok;
-}
 
 /* ---------------------------------------------------------------------------
  * level 0: weighing.  Per step: panel [H | -F | c] (n x (2n+1)) weighed by K's
@@ -314,7 +154,7 @@ __global__ void __launch_bounds__(NT) pair_cta(CArgs a)
         A[e] = v;
       }
       __syncthreads();
-      householder(A, ld, rows, n, ld, red);
+      ::cta::householder(A, ld, rows, n, ld, red);
       for (int e = tid; e < n * n; e += NT) {
         const int r = e / n, c = e - r * n; /* R~ (r, c), Y~ (r, c) */
         Rr.R.at(c * n + r, se) = r <= c ? A[(int64_t)r * ld + c] : 0.0;
@@ -339,7 +179,7 @@ __global__ void __launch_bounds__(NT) pair_cta(CArgs a)
                       : (c < n ? C.G.at(c * mx + (r - mj), sj1) : C.o.at(r - mj, sj1));
       }
       __syncthreads();
-      householder(A, ld, rows, n, ld, red);
+      ::cta::householder(A, ld, rows, n, ld, red);
       const int g2 = rows < n ? rows : n;
       for (int e = tid; e < g2 * n; e += NT) {
         const int r = e / n, c = e - r * n;
@@ -370,7 +210,7 @@ __global__ void __launch_bounds__(NT) pair_cta(CArgs a)
         A[e] = v;
       }
       __syncthreads();
-      householder(A, ld, rows, n, ld, red);
+      ::cta::householder(A, ld, rows, n, ld, red);
       for (int e = tid; e < n * n; e += NT) {
         const int r = e / n, c = e - r * n;
         Rr.R.at(c * n + r, se) = r <= c ? A[(int64_t)r * ld + c] : 0.0;
@@ -422,7 +262,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs a)
         A[e] = c < n ? C.G.at(c * mx + r, sb) : C.o.at(r, sb);
       }
       __syncthreads();
-      householder(A, ld, m0, n, ld, red);
+      ::cta::householder(A, ld, m0, n, ld, red);
       if (tid == 0)
         for (int i = 0; i < n; ++i)
           if (A[(int64_t)i * ld + i] == 0.0) atomicOr(a.flag, 2);
@@ -462,7 +302,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs a)
         WS[e] = c < n ? C.G.at(c * mx + r, s) : C.o.at(r, s);
       }
       __syncthreads();
-      householder(WS, ldA, ms, n, ldA, red);
+      ::cta::householder(WS, ldA, ms, n, ldA, red);
     }
     for (int e = tid; e < rowsT * ldT; e += NT) {
       const int r = e / ldT, c = e - r * ldT;
@@ -475,7 +315,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs a)
       WT[e] = v;
     }
     __syncthreads();
-    householder(WT, ldT, rowsT, n, ldT, red);
+    ::cta::householder(WT, ldT, rowsT, n, ldT, red);
     for (int e = tid; e < n * n; e += NT) {
       const int r = e / n, c = e - r * n;
       Rr.R.at(c * n + r, es) = r <= c ? WT[(int64_t)r * ldT + c] : 0.0;
@@ -499,7 +339,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs a)
                      : (c < n ? WT[(int64_t)(n + r - gp) * ldT + n + c] : WT[(int64_t)(n + r - gp) * ldT + 2 * n]);
     }
     __syncthreads();
-    householder(WF, ldF, rF, n, ldF, red);
+    ::cta::householder(WF, ldF, rF, n, ldF, red);
     const int g2 = rF < n ? rF : n;
     for (int e = tid; e < g2 * n; e += NT) {
       const int r = e / n, c = e - r * n;
@@ -621,4 +461,4 @@ __global__ void __launch_bounds__(NT) solve_cta(CArgs a, int want_cov)
   }
 }
 
-}  // namespace cta
+}  // namespace ctak
