@@ -138,6 +138,29 @@ double  kalman_gpu_measure_fp32_tflops(void);
 #define KALMAN_GPU_NOALLOC_SCRATCH_BYTES (64u << 20)
 int kalman_gpu_smooth_oddeven_noalloc(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream);
 
+/* Prepared plans, replayed as CUDA graphs.  No counterpart in the reference
+ * (which rebuilds its step structures on every call).
+ *
+ * For callers that smooth problems of one fixed shape again and again (a
+ * tracker re-smoothing a sliding window of the same length every frame, a
+ * service with a few fixed request sizes): kalman_gpu_plan_create takes a
+ * problem of device arrays (location KALMAN_GPU_DEVICE), builds the plan
+ * tables into a workspace the plan owns and captures the whole launch
+ * sequence into a CUDA graph.  kalman_gpu_plan_execute replays it on a stream
+ * -- asynchronously, with the current contents of the same device arrays, so
+ * the caller refills them between executions; the track lengths, n, mmax,
+ * the array addresses and the options are those of the creation.
+ * kalman_gpu_plan_status waits for the last execution and returns its status
+ * (the KALMAN_GPU_* codes above).  create returns NULL on failure (see
+ * kalman_gpu_last_error).  A plan belongs to the device current at its
+ * creation; executions of one plan must not overlap on the GPU (they share
+ * its workspace). */
+typedef struct kalman_gpu_plan kalman_gpu_plan_t;
+kalman_gpu_plan_t* kalman_gpu_plan_create(uint32_t options, const kalman_gpu_problem_t* p);
+int kalman_gpu_plan_execute(kalman_gpu_plan_t* plan, void* cuda_stream);
+int kalman_gpu_plan_status(kalman_gpu_plan_t* plan);
+void kalman_gpu_plan_destroy(kalman_gpu_plan_t* plan);
+
 /* Releases the device workspace and pinned staging buffers cached by the
  * library for the current device.                                            */
 void kalman_gpu_release(void);

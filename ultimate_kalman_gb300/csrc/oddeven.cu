@@ -2515,7 +2515,7 @@ __global__ void upload_tables_kernel(int64_t* __restrict__ dst, const int64_t* _
  * (uploaded with cudaMemcpyAsync) */
 template <typename T>
 int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, const Plan& P, const int64_t* tab,
-             char* B, const int64_t* tab_dev = nullptr)
+             char* B, const int64_t* tab_dev = nullptr, bool enqueue_only = false)
 {
   const int n = p->n, T_ = p->ntracks, nlev = P.nlev;
   const int mx = p->mmax > n ? p->mmax : n;
@@ -2527,7 +2527,7 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
   if (tab_dev)
     upload_tables_kernel<<<(unsigned)std::min<size_t>((P.tab_entries + 255) / 256, 1024), 256, 0, st>>>(
         dtab, tab_dev, (int64_t)P.tab_entries);
-  else
+  else if (tab) /* null: the tables are already in the workspace */
     cudaMemcpyAsync(dtab, tab, P.tab_entries * sizeof(int64_t), cudaMemcpyHostToDevice, st);
   cudaMemsetAsync(dflag, 0, sizeof(int), st);
 
@@ -2767,6 +2767,7 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
       UKG_LAUNCH(UKG_K_REFINE, st, (add_kernel<<<grid(cnt, 256), 256, 0, st>>>(p->state, dx, cnt)));
     }
   }
+  if (enqueue_only) return 0;
   int hflag = 0;
   cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaError_t e = cudaStreamSynchronize(st);
@@ -2880,7 +2881,8 @@ int cta_count()
 }
 
 int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, const Plan& P,
-                 const int64_t* tab_dev, char* B, double* scratch, int64_t per_cta, int ncta)
+                 const int64_t* tab_dev, char* B, double* scratch, int64_t per_cta, int ncta,
+                 bool enqueue_only = false)
 {
   const int n = p->n, T_ = p->ntracks, nlev = P.nlev;
   const int mx = p->mmax > n ? p->mmax : n;
@@ -2889,8 +2891,9 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
   const LevelPlan* lp = P.lp;
   int64_t* dtab = (int64_t*)(B + P.o_tab);
   int* dflag = (int*)(B + P.o_flag);
-  upload_tables_kernel<<<(unsigned)std::min<size_t>((P.tab_entries + 255) / 256, 1024), 256, 0, st>>>(
-      dtab, tab_dev, (int64_t)P.tab_entries);
+  if (tab_dev) /* null: the tables are already in the workspace */
+    upload_tables_kernel<<<(unsigned)std::min<size_t>((P.tab_entries + 255) / 256, 1024), 256, 0, st>>>(
+        dtab, tab_dev, (int64_t)P.tab_entries);
   cudaMemsetAsync(dflag, 0, sizeof(int), st);
   auto tables = [&](int l) {
     Tables d;
@@ -2974,6 +2977,7 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
       UKG_LAUNCH(UKG_K_SOLVE, st,
                  (ctak::solve_cta<<<grid(lp[l].nsolve), cta::NT, 0, st>>>(a, want_cov ? 1 : 0)));
   }
+  if (enqueue_only) return 0;
   int hflag = 0;
   cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaError_t e = cudaStreamSynchronize(st);
@@ -3098,4 +3102,150 @@ extern "C" int kalman_gpu_smooth_oddeven_noalloc(uint32_t options, const kalman_
                                       g_noalloc_tab, (char*)g_noalloc_addr[dev]);
   ukg_prof_resume(prof);
   return status;
+}
+
+/* ---------------------------------------------------------------------------
+ * Prepared plans replayed as CUDA graphs (kalman_gpu_plan_*).
+ *
+ * For callers that smooth problems of one fixed shape again and again -- a
+ * tracker re-smoothing a sliding window of the same length every frame, a
+ * service whose requests come in a few fixed sizes -- every host step of a
+ * call (plan tables, workspace, launch configuration, a hundred-odd kernel
+ * launches) is done once: the tables are uploaded to a workspace the plan
+ * owns and the whole launch sequence is captured into a CUDA graph; each
+ * execution is one graph launch on the caller's stream, asynchronous, with
+ * the current contents of the caller's device arrays.  The reference has no
+ * counterpart (it rebuilds its step structures on every call).
+ * ------------------------------------------------------------------------ */
+struct kalman_gpu_plan {
+  int device = -1;
+  bool cta = false;
+  void* work = nullptr;
+  int* dflag = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t last = nullptr;
+  bool launched = false;
+};
+
+extern "C" void kalman_gpu_plan_destroy(kalman_gpu_plan_t* pl)
+{
+  if (!pl) return;
+  if (pl->launched) cudaStreamSynchronize(pl->last);
+  if (pl->exec) cudaGraphExecDestroy(pl->exec);
+  if (pl->graph) cudaGraphDestroy(pl->graph);
+  if (pl->work) cudaFree(pl->work);
+  delete pl;
+}
+
+extern "C" kalman_gpu_plan_t* kalman_gpu_plan_create(uint32_t options, const kalman_gpu_problem_t* p)
+{
+  ukg_clear_error();
+  if (ukg_validate_problem(p, 0)) return nullptr;
+  if (p->location != KALMAN_GPU_DEVICE) {
+    ukg_set_error(KALMAN_GPU_EINVAL, "a plan takes device arrays (it is replayed on their current contents)");
+    return nullptr;
+  }
+  if (p->nsteps == 0) {
+    ukg_set_error(KALMAN_GPU_EINVAL, "a plan needs at least one step");
+    return nullptr;
+  }
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    ukg_set_error(KALMAN_GPU_ENODEV, "no CUDA device is available");
+    return nullptr;
+  }
+  const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
+  const int mxp = p->mmax > p->n ? p->mmax : p->n;
+  const bool cta = p->n >= kCtaMinN || mxp > 8;
+  if (cta && mxp > kCtaMaxN) {
+    ukg_set_error(KALMAN_GPU_EINVAL, "state dimension %d (observation rows %d) above this build's limit %d", p->n,
+                  p->mmax, kCtaMaxN);
+    return nullptr;
+  }
+  const bool fp32 = !cta && (options & KALMAN_GPU_FP32_REFINE) != 0;
+  Plan P;
+  const size_t need = build_plan(p, want_cov, fp32, fp32, P, nullptr, 0);
+  if (need == 0) {
+    ukg_set_error(KALMAN_GPU_EINVAL, "tracks longer than 2^%d steps", kMaxLevels - 1);
+    return nullptr;
+  }
+  std::vector<int64_t> tab(need);
+  build_plan(p, want_cov, fp32, fp32, P, tab.data(), need);
+  kalman_gpu_plan* pl = new kalman_gpu_plan();
+  pl->cta = cta;
+  cudaGetDevice(&pl->device);
+  const int ncta = cta ? cta_count() : 0;
+  const int64_t per = cta ? cta_scratch_per_cta(p->n, p->mmax) : 0;
+  const size_t scratch_off = align_up(P.bytes, 256);
+  const size_t bytes = cta ? scratch_off + (size_t)ncta * per * sizeof(double) : P.bytes;
+  cudaError_t e = cudaMalloc(&pl->work, bytes);
+  if (e == cudaSuccess)
+    e = cudaMemcpy((char*)pl->work + P.o_tab, tab.data(), need * sizeof(int64_t), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    ukg_set_error(KALMAN_GPU_ENOMEM, "plan workspace of %zu bytes: %s", bytes, cudaGetErrorString(e));
+    kalman_gpu_plan_destroy(pl);
+    return nullptr;
+  }
+  pl->dflag = (int*)((char*)pl->work + P.o_flag);
+  cudaStream_t cs = nullptr;
+  e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) {
+    const int prof = ukg_prof_pause(); /* no profiling events inside the graph */
+    int st;
+    if (cta)
+      st = run_plan_cta(options, p, cs, P, nullptr, (char*)pl->work, (double*)((char*)pl->work + scratch_off), per,
+                        ncta, true);
+    else if (fp32)
+      st = run_plan<float>(options, p, cs, P, nullptr, (char*)pl->work, nullptr, true);
+    else
+      st = run_plan<double>(options, p, cs, P, nullptr, (char*)pl->work, nullptr, true);
+    ukg_prof_resume(prof);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(cs, &g);
+    pl->graph = g;
+    e = st ? cudaErrorUnknown : ee;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&pl->exec, pl->graph, 0);
+  if (cs) cudaStreamDestroy(cs);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    if (!kalman_gpu_last_status())
+      ukg_set_error(KALMAN_GPU_ECUDA, "capturing the plan into a CUDA graph: %s", cudaGetErrorString(e));
+    kalman_gpu_plan_destroy(pl);
+    return nullptr;
+  }
+  return pl;
+}
+
+extern "C" int kalman_gpu_plan_execute(kalman_gpu_plan_t* pl, void* cuda_stream)
+{
+  ukg_clear_error();
+  if (!pl || !pl->exec) return ukg_set_error(KALMAN_GPU_EINVAL, "no plan");
+  cudaStream_t st = (cudaStream_t)cuda_stream;
+  const cudaError_t e = cudaGraphLaunch(pl->exec, st);
+  if (e != cudaSuccess) return ukg_set_error(KALMAN_GPU_ECUDA, "plan launch: %s", cudaGetErrorString(e));
+  pl->last = st;
+  pl->launched = true;
+  return 0;
+}
+
+extern "C" int kalman_gpu_plan_status(kalman_gpu_plan_t* pl)
+{
+  ukg_clear_error();
+  if (!pl || !pl->exec) return ukg_set_error(KALMAN_GPU_EINVAL, "no plan");
+  if (!pl->launched) return 0;
+  int hflag = 0;
+  cudaError_t e = cudaStreamSynchronize(pl->last);
+  if (e == cudaSuccess) e = cudaMemcpy(&hflag, pl->dflag, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return ukg_set_error(KALMAN_GPU_ECUDA, "plan: %s", cudaGetErrorString(e));
+  if (hflag & 8) return ukg_set_error(KALMAN_GPU_ECUDA, "a bulk copy into shared memory did not complete in time");
+  if (hflag & 4) return ukg_set_error(KALMAN_GPU_EINVAL, "malformed input: observation rows outside [0, mmax] or an "
+                                     "unknown covariance type");
+  if (hflag & 1) return ukg_set_error(KALMAN_GPU_ESINGULAR, "a covariance factor is not positive definite");
+  if (hflag & 2) return ukg_set_error(KALMAN_GPU_ESINGULAR, "zero pivot: the smoothing problem is not observable");
+  return 0;
 }

@@ -85,6 +85,7 @@ EXPORTED = [
     "kalman_gpu_smooth_oddeven_packed", "kalman_gpu_smooth_associative_packed", "kalman_gpu_smooth_tracks",
     "kalman_gpu_release", "kalman_gpu_profile_enable", "kalman_gpu_profile_read", "kalman_gpu_launch_count",
     "kalman_gpu_measure_fp64_tflops", "kalman_gpu_measure_fp32_tflops", "kalman_gpu_smooth_oddeven_noalloc",
+    "kalman_gpu_plan_create", "kalman_gpu_plan_execute", "kalman_gpu_plan_status", "kalman_gpu_plan_destroy",
 ]
 
 _lib = None
@@ -119,6 +120,13 @@ def load(path=LIB_PATH):
     L.kalman_gpu_measure_fp64_tflops.argtypes = [ctypes.c_int]
     L.kalman_gpu_measure_fp64_tflops.restype = ctypes.c_double
     L.kalman_gpu_measure_fp32_tflops.restype = ctypes.c_double
+    L.kalman_gpu_plan_create.argtypes = [ctypes.c_uint32, P]
+    L.kalman_gpu_plan_create.restype = ctypes.c_void_p
+    L.kalman_gpu_plan_execute.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    L.kalman_gpu_plan_execute.restype = ctypes.c_int
+    L.kalman_gpu_plan_status.argtypes = [ctypes.c_void_p]
+    L.kalman_gpu_plan_status.restype = ctypes.c_int
+    L.kalman_gpu_plan_destroy.argtypes = [ctypes.c_void_p]
     _lib = L
     return L
 
@@ -212,12 +220,53 @@ class DeviceProblem:
             _check(status)
         return status
 
+    def plan(self, algorithm="oddeven", covariance=True, fp32_refine=False, sweeps=0):
+        """A CUDA-graph plan over these device arrays (odd-even only): see
+        kalman_gpu_plan_create.  Returns a Plan; refill the arrays in place
+        between executions."""
+        if algorithm != "oddeven":
+            raise ValueError("plans cover the odd-even smoother")
+        L = load()
+        opts = options_for(algorithm, covariance and self.cov is not None, fp32_refine, sweeps)
+        h = L.kalman_gpu_plan_create(opts, ctypes.byref(self.struct))
+        if not h:
+            _check(L.kalman_gpu_last_status())
+        return Plan(h, self)
+
     def results(self):
         X = self.state.cpu().numpy()
         S = None
         if self.cov is not None:
             S = np.ascontiguousarray(self.cov.cpu().numpy().transpose(0, 2, 1))
         return X, S
+
+
+class Plan:
+    """A prepared odd-even plan replayed as a CUDA graph (kalman_gpu_plan_*)."""
+
+    def __init__(self, handle, owner):
+        self.h = handle
+        self.owner = owner  # keeps the device arrays alive
+
+    def execute(self, stream=None):
+        L = load()
+        import torch
+        st = stream if stream is not None else torch.cuda.current_stream()
+        _check(L.kalman_gpu_plan_execute(self.h, ctypes.c_void_p(st.cuda_stream)))
+
+    def status(self):
+        return load().kalman_gpu_plan_status(self.h)
+
+    def close(self):
+        if self.h:
+            load().kalman_gpu_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def smooth(P, algorithm="oddeven", covariance=True, fp32_refine=False, location="device", sweeps=0):
