@@ -1,0 +1,111 @@
+"""The serving loop (ultimate_kalman_gb300/serve.py): scheduling rules on a
+simulated clock (CPU), and on the GPU, results of requests served in mixed
+batches equal the same requests smoothed alone (bit-equal: tracks are
+independent, so a batch does not change a track's arithmetic)."""
+import numpy as np
+import pytest
+
+from ultimate_kalman_gb300 import serve
+
+
+class FakeExecutor:
+    """Records uploads and batches; the clock advances by the batch's steps."""
+
+    def __init__(self, clock, rate=1e6):
+        self.clock, self.rate = clock, rate
+        self.resident = set()
+        self.batches = []
+
+    def upload(self, r):
+        self.resident.add(r.rid)
+
+    def release(self, r):
+        self.resident.discard(r.rid)
+
+    def run(self, batch):
+        assert all(r.rid in self.resident for r in batch)
+        self.batches.append([r.rid for r in batch])
+        self.clock.t += sum(r.steps for r in batch) / self.rate
+        for r in batch:
+            r.state = np.zeros((r.steps, r.problem.n))
+
+
+class Clock:
+    t = 0.0
+
+    def __call__(self):
+        return self.t
+
+    def wait(self, dt):
+        self.t += max(dt, 1e-6)
+
+
+def make_stream(nreq=40, rate=200.0, seed=3):
+    return serve.request_stream(nreq, rate, seed=seed, dims=(4, 6, 12), min_len=64, max_len=600)
+
+
+def test_admission_respects_the_budget_and_every_request_completes():
+    clock = Clock()
+    reqs = make_stream()
+    budget = 3 * max(serve.footprint(r) for r in reqs)
+    ex = FakeExecutor(clock)
+    srv = serve.Server(ex, hbm_budget=budget, clock=clock, wait=clock.wait)
+    done = srv.serve(reqs)
+    assert sorted(r.rid for r in done) == list(range(len(reqs)))
+    assert srv.peak_in_use <= budget
+    assert srv.in_use == 0 and not ex.resident
+    for r in done:
+        assert r.admitted >= r.arrival and r.completed >= r.admitted
+
+
+def test_batches_are_one_shape_class_in_arrival_order():
+    clock = Clock()
+    reqs = make_stream(nreq=60, rate=2000.0)
+    by_id = {r.rid: r for r in reqs}
+    ex = FakeExecutor(clock, rate=2e5)
+    srv = serve.Server(ex, hbm_budget=1 << 40, clock=clock, wait=clock.wait)
+    srv.serve(reqs)
+    for b in ex.batches:
+        keys = {by_id[i].key() for i in b}
+        assert len(keys) == 1
+        arr = [by_id[i].arrival for i in b]
+        assert arr == sorted(arr)
+    assert max(len(b) for b in ex.batches) > 1  # requests were batched
+
+
+def test_batch_step_limit():
+    clock = Clock()
+    reqs = make_stream(nreq=30, rate=1e5)
+    ex = FakeExecutor(clock)
+    limit = 1500
+    srv = serve.Server(ex, hbm_budget=1 << 40, max_batch_steps=limit, clock=clock, wait=clock.wait)
+    srv.serve(reqs)
+    by_id = {r.rid: r for r in reqs}
+    for b in ex.batches:
+        steps = sum(by_id[i].steps for i in b)
+        assert steps <= limit or len(b) == 1
+
+
+def test_request_larger_than_the_budget_is_refused():
+    clock = Clock()
+    reqs = make_stream(nreq=3)
+    srv = serve.Server(FakeExecutor(clock), hbm_budget=16, clock=clock, wait=clock.wait)
+    with pytest.raises(ValueError):
+        srv.serve(reqs)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fp32", [False, True])
+def test_served_results_equal_results_alone(fp32):
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    from ultimate_kalman_gb300 import native
+    reqs = serve.request_stream(24, 1e6, seed=11, dims=(4, 6, 12), min_len=64, max_len=3000, fp32_refine=fp32)
+    ex = serve.GpuExecutor()
+    srv = serve.Server(ex, hbm_budget=1 << 32)
+    done = srv.serve(reqs)
+    assert len(srv.batches) < len(reqs)  # some requests shared a batch
+    for r in done:
+        X, _ = native.smooth(r.problem, covariance=False, fp32_refine=fp32)
+        np.testing.assert_array_equal(r.state, X)
