@@ -1,0 +1,90 @@
+"""Times one smoothing of a single synthetic track of a given shape on the GPU
+(the larger-state configurations: n=48/m=24 for the associative smoother,
+n=128/m=64 for the odd-even smoother, n in {4, 6, 12, 24} for serving).
+
+The track follows the configurations' recipe: F = rho Q (Q random orthogonal),
+H = I, G i.i.d. N(0, 1/m), SPD noise covariances with eigenvalues in [lo, hi]
+(log-uniform with --log-cov), a square step-0 observation, a fraction of
+steps without observation.  Matrices are shared along the track (the work does
+not depend on their values), so large k is cheap to build.
+
+    python -m ultimate_kalman_gb300.shapes --n 48 --m 24 --k 100000 --algorithm associative
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import numpy as np
+
+from . import problem as pb
+
+
+def synthetic_track(k, n, m, rho=0.99, lo=0.1, hi=1.0, log_cov=False, missing=0.05, seed=0):
+    rng = np.random.default_rng(seed)
+    P = pb.empty_problem(n, max(n, m), [k])
+    mx = max(n, m)
+    Fm = rho * pb.random_orthogonal(rng, n)
+    Gm = rng.standard_normal((m, n)) / np.sqrt(m)
+    Kc = pb.random_spd(rng, n, lo, hi, log_cov)
+    Cc = pb.random_spd(rng, m, lo, hi, log_cov)
+    P.H[1:] = np.eye(n)
+    P.F[1:] = Fm.T
+    P.K[1:] = Kc.T
+    Gt = np.zeros((n, mx))
+    Gt[:, :m] = Gm.T
+    Ct = np.zeros((mx, mx))
+    Ct[:m, :m] = Cc.T
+    P.G[1:] = Gt
+    P.C[1:] = Ct
+    P.o[1:, :m] = rng.standard_normal((k - 1, m))
+    P.obs_rows[1:] = m
+    if missing > 0:
+        P.obs_rows[1:][rng.random(k - 1) < missing] = 0
+    G0 = np.zeros((n, mx))
+    G0[:, :n] = np.eye(n)
+    C0 = np.zeros((mx, mx))
+    C0[:n, :n] = np.eye(n)
+    P.G[0], P.C[0] = G0, C0
+    P.o[0, :n] = rng.standard_normal(n)
+    P.obs_rows[0] = n
+    return P
+
+
+def main():
+    import torch
+    from . import native
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--n", type=int, default=48)
+    ap.add_argument("--m", type=int, default=24)
+    ap.add_argument("--k", type=int, default=100000)
+    ap.add_argument("--algorithm", default="associative", choices=["oddeven", "associative"])
+    ap.add_argument("--no-covariance", action="store_true")
+    ap.add_argument("--repeats", type=int, default=3)
+    ap.add_argument("--log-cov", action="store_true", help="covariance eigenvalues log-uniform in [1e-3, 1]")
+    args = ap.parse_args()
+    lo = 1e-3 if args.log_cov else 0.1
+    P = synthetic_track(args.k, args.n, args.m, lo=lo, log_cov=args.log_cov,
+                        rho=0.995 if args.n >= 128 else 0.99)
+    cov = not args.no_covariance
+    D = native.DeviceProblem(P, covariance=cov)
+    D.smooth(args.algorithm, covariance=cov)
+    torch.cuda.synchronize()
+    native.profile_enable(True)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(args.repeats):
+        D.smooth(args.algorithm, covariance=cov)
+    e.record()
+    torch.cuda.synchronize()
+    prof = native.profile_read()
+    native.profile_enable(False)
+    ms = s.elapsed_time(e) / args.repeats
+    print(json.dumps({"algorithm": args.algorithm, "n": args.n, "m": args.m, "k": args.k, "covariance": cov,
+                      "ms": ms, "steps_per_s": args.k / (ms * 1e-3),
+                      "per_kernel_ms": {k2: v[0] / args.repeats for k2, v in prof.items()},
+                      "input_gb": D.input_bytes() / 1e9}))
+
+
+if __name__ == "__main__":
+    main()
