@@ -56,3 +56,14 @@ def test_batched_and_full_size():
     X, _ = run(P)
     st, Xo, _ = oracle.smooth(P, "oddeven", covariance=False)
     assert oracle.rel_err_states(X, Xo) < TOL_STATE
+
+
+@pytest.mark.parametrize("n,k", [(9, 60), (12, 200), (24, 90), (48, 40)])
+def test_precision_form_larger_states(n, k):
+    """FP32 CTA factorization + FP64 refinement for state dimensions past 8:
+    states within 1e-9 of the oracle."""
+    P = pb.random_dynamics([k, 37, 1, 2], n, n // 2, seed=30 + n, per_step=True, missing=0.1)
+    X, _ = native.smooth(P, covariance=False, fp32_refine=True)
+    st, Xo, _ = oracle.smooth(P, "oddeven", covariance=False)
+    assert st == 0
+    assert oracle.rel_err_states(X, Xo) < 1e-9

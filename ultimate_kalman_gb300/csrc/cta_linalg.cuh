@@ -4,7 +4,7 @@
  * with one thread per column, triangular solves with one thread per
  * right-hand side, weighing by a covariance factor.  Used by the CTA kernels
  * of the odd-even and associative smoothers for larger state dimensions.
- * FP64.
+ * Templates over the arithmetic type (FP64, or FP32 for the precision form).
  */
 #pragma once
 #include <cstdint>
@@ -12,6 +12,7 @@
 namespace cta {
 
 constexpr int NT = 128; /* threads per CTA; rows of a panel beyond NT are looped */
+constexpr int kMaxPanelRows = 256; /* 2 x the largest state dimension (128) */
 
 /* slot-major view: entry e of slot s at p[s * w + e] */
 template <typename T>
@@ -20,20 +21,21 @@ struct Aos {
   int64_t w;
   __device__ __forceinline__ T& at(int e, int64_t s) const { return p[s * w + e]; }
 };
-/* sum over the CTA, returned to every thread; red holds >= 33 doubles */
-static __device__ __forceinline__ double block_sum(double v, double* red)
+/* sum over the CTA, returned to every thread; red holds >= 33 entries */
+template <typename T>
+static __device__ __forceinline__ T block_sum(T v, T* red)
 {
   for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) red[warp] = v;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0.0;
+    T s = T(0);
     for (int w = 0; w < NT / 32; ++w) s += red[w];
     red[32] = s;
   }
   __syncthreads();
-  const double r = red[32];
+  const T r = red[32];
   __syncthreads(); /* red may be reused right away */
   return r;
 }
@@ -41,31 +43,47 @@ static __device__ __forceinline__ double block_sum(double v, double* red)
 /* Householder QR of the row-major panel A (ld) on its first `rows` rows: the
  * first npiv columns are triangularized (reflectors stored below the
  * diagonal, LAPACK dlarfg convention), Q^T is applied to all `cols` columns. */
-static __device__ void householder(double* A, int ld, int rows, int npiv, int cols, double* red)
+template <typename T>
+static __device__ void householder(T* A, int ld, int rows, int npiv, int cols, T* red)
 {
+  __shared__ T vs[kMaxPanelRows];
   const int tid = threadIdx.x;
   const int kmax = rows < npiv ? rows : npiv;
   for (int k = 0; k < kmax; ++k) {
-    double part = 0.0;
+    T part = T(0);
     for (int i = k + 1 + tid; i < rows; i += NT) {
-      const double x = A[(int64_t)i * ld + k];
+      const T x = A[(int64_t)i * ld + k];
       part = fma(x, x, part);
     }
-    const double tail = block_sum(part, red);
-    const double alpha = A[(int64_t)k * ld + k];
-    if (tail == 0.0) continue; /* identity reflector: every thread agrees */
-    const double beta = -copysign(sqrt(fma(alpha, alpha, tail)), alpha);
-    const double amb = alpha - beta;
-    const double inv = 1.0 / (beta * amb);
-    const double t = -(amb * amb) * inv, scale = beta * inv;
-    for (int i = k + 1 + tid; i < rows; i += NT) A[(int64_t)i * ld + k] *= scale;
+    const T tail = block_sum(part, red);
+    const T alpha = A[(int64_t)k * ld + k];
+    if (tail == T(0)) continue; /* identity reflector: every thread agrees */
+    const T beta = -copysign(sqrt(fma(alpha, alpha, tail)), alpha);
+    const T amb = alpha - beta;
+    const T inv = T(1) / (beta * amb);
+    const T t = -(amb * amb) * inv, scale = beta * inv;
+    /* the reflector goes to shared memory too: every column update reads it */
+    for (int i = k + 1 + tid; i < rows; i += NT) {
+      const T v = A[(int64_t)i * ld + k] * scale;
+      A[(int64_t)i * ld + k] = v;
+      vs[i] = v;
+    }
     __syncthreads();
     for (int j = k + 1 + tid; j < cols; j += NT) {
-      double d = A[(int64_t)k * ld + j];
-      for (int i = k + 1; i < rows; ++i) d = fma(A[(int64_t)i * ld + k], A[(int64_t)i * ld + j], d);
+      /* four partial sums: independent FMA chains */
+      T d0 = A[(int64_t)k * ld + j], d1 = T(0), d2 = T(0), d3 = T(0);
+      int i = k + 1;
+      for (; i + 3 < rows; i += 4) {
+        d0 = fma(vs[i], A[(int64_t)i * ld + j], d0);
+        d1 = fma(vs[i + 1], A[(int64_t)(i + 1) * ld + j], d1);
+        d2 = fma(vs[i + 2], A[(int64_t)(i + 2) * ld + j], d2);
+        d3 = fma(vs[i + 3], A[(int64_t)(i + 3) * ld + j], d3);
+      }
+      for (; i < rows; ++i) d0 = fma(vs[i], A[(int64_t)i * ld + j], d0);
+      T d = (d0 + d1) + (d2 + d3);
       d *= t;
       A[(int64_t)k * ld + j] -= d;
-      for (int i = k + 1; i < rows; ++i) A[(int64_t)i * ld + j] = fma(-d, A[(int64_t)i * ld + k], A[(int64_t)i * ld + j]);
+      for (int i = k + 1; i < rows; ++i) A[(int64_t)i * ld + j] = fma(-d, vs[i], A[(int64_t)i * ld + j]);
     }
     if (tid == 0) A[(int64_t)k * ld + k] = beta;
     __syncthreads();
@@ -74,24 +92,31 @@ static __device__ void householder(double* A, int ld, int rows, int npiv, int co
 
 /* x <- R^{-1} x for every column c0 <= c < c1 of the row-major X (ldx), R the
  * upper triangle of the row-major Rm (ldr), n x n: one thread per column */
-static __device__ void solve_upper_cols(const double* Rm, int ldr, int n, double* X, int ldx, int c0, int c1)
+template <typename T>
+static __device__ void solve_upper_cols(const T* Rm, int ldr, int n, T* X, int ldx, int c0, int c1)
 {
   for (int c = c0 + threadIdx.x; c < c1; c += NT)
     for (int i = n - 1; i >= 0; --i) {
-      double s = X[(int64_t)i * ldx + c];
-      for (int k = i + 1; k < n; ++k) s = fma(-Rm[(int64_t)i * ldr + k], X[(int64_t)k * ldx + c], s);
-      X[(int64_t)i * ldx + c] = s / Rm[(int64_t)i * ldr + i];
+      T s0 = X[(int64_t)i * ldx + c], s1 = T(0);
+      int k = i + 1;
+      for (; k + 1 < n; k += 2) {
+        s0 = fma(-Rm[(int64_t)i * ldr + k], X[(int64_t)k * ldx + c], s0);
+        s1 = fma(-Rm[(int64_t)i * ldr + k + 1], X[(int64_t)(k + 1) * ldx + c], s1);
+      }
+      if (k < n) s0 = fma(-Rm[(int64_t)i * ldr + k], X[(int64_t)k * ldx + c], s0);
+      X[(int64_t)i * ldx + c] = (s0 + s1) / Rm[(int64_t)i * ldr + i];
     }
   __syncthreads();
 }
 
 /* x <- R^{-1} x for one vector x (n entries, shared by the CTA) */
-static __device__ void solve_upper_vec(const double* Rm, int ldr, int n, double* x)
+template <typename T>
+static __device__ void solve_upper_vec(const T* Rm, int ldr, int n, T* x)
 {
   for (int i = n - 1; i >= 0; --i) {
     if (threadIdx.x == 0) x[i] /= Rm[(int64_t)i * ldr + i];
     __syncthreads();
-    const double xi = x[i];
+    const T xi = x[i];
     for (int k = threadIdx.x; k < i; k += NT) x[k] = fma(-Rm[(int64_t)k * ldr + i], xi, x[k]);
     __syncthreads();
   }
@@ -104,14 +129,15 @@ static __device__ __forceinline__ bool valid_cov_type(char t) { return t == 'W' 
  * 'C' B <- chol(cov)^{-1} B, 'U'/'F' B <- tril(cov)^{-1} B.  L (rows x rows
  * row-major, ld rows) is scratch.  Returns false (in every thread) for a
  * factor that is not positive definite or has a zero pivot. */
-static __device__ bool weigh_panel(char type, const double* cov, int ldc, int rows, double* B, int ldb, int cols, double* L,
-                            double* red, double* tmp)
+template <typename T>
+static __device__ bool weigh_panel(char type, const double* cov, int ldc, int rows, T* B, int ldb, int cols, T* L,
+                                  T* red, T* tmp)
 {
   const int tid = threadIdx.x;
   if (type == 'w') {
     for (int e = tid; e < rows * cols; e += NT) {
       const int i = e / cols, c = e - i * cols;
-      B[(int64_t)i * ldb + c] *= cov[i];
+      B[(int64_t)i * ldb + c] *= T(cov[i]);
     }
     __syncthreads();
     return true;
@@ -119,8 +145,8 @@ static __device__ bool weigh_panel(char type, const double* cov, int ldc, int ro
   if (type == 'W') { /* B <- W B, one thread per column, W read from the caller's array */
     for (int c = tid; c < cols; c += NT) {
       for (int i = 0; i < rows; ++i) {
-        double s = 0.0;
-        for (int j = 0; j < rows; ++j) s = fma(cov[(int64_t)j * ldc + i], B[(int64_t)j * ldb + c], s);
+        T s = T(0);
+        for (int j = 0; j < rows; ++j) s = fma(T(cov[(int64_t)j * ldc + i]), B[(int64_t)j * ldb + c], s);
         tmp[(int64_t)i * NT + tid] = s;
       }
       for (int i = 0; i < rows; ++i) B[(int64_t)i * ldb + c] = tmp[(int64_t)i * NT + tid];
@@ -131,7 +157,7 @@ static __device__ bool weigh_panel(char type, const double* cov, int ldc, int ro
   if (type != 'C' && type != 'U' && type != 'F') return true;
   for (int e = tid; e < rows * rows; e += NT) {
     const int i = e / rows, j = e - i * rows;
-    L[e] = i >= j ? cov[(int64_t)j * ldc + i] : 0.0;
+    L[e] = i >= j ? T(cov[(int64_t)j * ldc + i]) : T(0);
   }
   __syncthreads();
   __shared__ int bad_s;
@@ -140,16 +166,16 @@ static __device__ bool weigh_panel(char type, const double* cov, int ldc, int ro
   if (type == 'C') { /* right-looking Cholesky, in place in L */
     for (int j = 0; j < rows; ++j) {
       if (tid == 0) {
-        const double d = L[(int64_t)j * rows + j];
-        if (!(d > 0.0)) bad_s = 1;
-        L[(int64_t)j * rows + j] = d > 0.0 ? sqrt(d) : 1.0;
+        const T d = L[(int64_t)j * rows + j];
+        if (!(d > T(0))) bad_s = 1;
+        L[(int64_t)j * rows + j] = d > T(0) ? sqrt(d) : T(1);
       }
       __syncthreads();
-      const double ljj = L[(int64_t)j * rows + j];
+      const T ljj = L[(int64_t)j * rows + j];
       for (int i = j + 1 + tid; i < rows; i += NT) L[(int64_t)i * rows + j] /= ljj;
       __syncthreads();
       for (int i = j + 1 + tid; i < rows; i += NT) {
-        const double lij = L[(int64_t)i * rows + j];
+        const T lij = L[(int64_t)i * rows + j];
         for (int l = j + 1; l <= i; ++l) L[(int64_t)i * rows + l] = fma(-lij, L[(int64_t)l * rows + j], L[(int64_t)i * rows + l]);
       }
       __syncthreads();
@@ -157,13 +183,13 @@ static __device__ bool weigh_panel(char type, const double* cov, int ldc, int ro
   } else {
     if (tid == 0)
       for (int j = 0; j < rows; ++j)
-        if (L[(int64_t)j * rows + j] == 0.0) bad_s = 1;
+        if (L[(int64_t)j * rows + j] == T(0)) bad_s = 1;
     __syncthreads();
   }
   /* forward substitution, one thread per column */
   for (int c = tid; c < cols; c += NT)
     for (int i = 0; i < rows; ++i) {
-      double s = B[(int64_t)i * ldb + c];
+      T s = B[(int64_t)i * ldb + c];
       for (int k = 0; k < i; ++k) s = fma(-L[(int64_t)i * rows + k], B[(int64_t)k * ldb + c], s);
       B[(int64_t)i * ldb + c] = s / L[(int64_t)i * rows + i];
     }

@@ -2880,8 +2880,9 @@ int cta_count()
   return std::max(sms, 1) * 4;
 }
 
+template <typename T>
 int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, const Plan& P,
-                 const int64_t* tab_dev, char* B, double* scratch, int64_t per_cta, int ncta,
+                 const int64_t* tab_dev, char* B, void* scratch, int64_t per_cta, int ncta,
                  bool enqueue_only = false)
 {
   const int n = p->n, T_ = p->ntracks, nlev = P.nlev;
@@ -2911,8 +2912,8 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
     return d;
   };
   auto eqa = [&](size_t off, size_t off_m, int64_t S) {
-    double* e = (double*)(B + off);
-    ctak::EqA<double> d;
+    T* e = (T*)(B + off);
+    ctak::EqA<T> d;
     d.F = {e, nn};
     d.H = {e + nn * S, nn};
     d.c = {e + 2 * nn * S, n};
@@ -2921,23 +2922,26 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
     d.m = (int32_t*)(B + off_m);
     return d;
   };
-  auto eq_level = [&](int l) { /* odd levels in their own region, even levels reuse level 0's */
-    return (l & 1) ? eqa(P.o_eqA, P.o_mA, P.S1) : eqa(P.o_eq0, P.o_m0, P.S0);
+  auto eq_level = [&](int l) { /* level 0; odd levels; even levels >= 2 (their own region in FP32) */
+    if (l == 0) return eqa(P.o_eq0, P.o_m0, P.S0);
+    if (l & 1) return eqa(P.o_eqA, P.o_mA, P.S1);
+    return P.fp32 ? eqa(P.o_eqB, P.o_mB, P.S2) : eqa(P.o_eq0, P.o_m0, P.S0);
   };
   auto rec = [&](int l) {
-    ctak::RecA<double> r;
+    ctak::RecA<T> r;
     memset(&r, 0, sizeof(r));
     if (l >= nlev) return r;
     const int64_t E = std::max<int64_t>(lp[l].E, 1);
-    double* d = (double*)(B + P.o_rec[l]);
+    T* d = (T*)(B + P.o_rec[l]);
     r.R = {d, nn};
     r.Ft = {d + nn * E, nn};
     r.Y = {d + 2 * nn * E, nn};
     r.rhs = {d + 3 * nn * E, n};
-    if (want_cov && l > 0) r.U = {(double*)(B + P.o_U[l]), nn};
+    if (want_cov && l > 0) r.U = {(T*)(B + P.o_U[l]), nn};
     return r;
   };
-  auto common = [&](ctak::CArgs& a, int l) {
+  Soa<T> baseR{P.refine ? (T*)(B + P.o_baseR) : nullptr, std::max(T_, 1)};
+  auto common = [&](ctak::CArgs<T>& a, int l) {
     memset(&a, 0, sizeof(a));
     a.ct = tables(l);
     a.nt = tables(l + 1);
@@ -2951,31 +2955,100 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
     a.state = p->state;
     a.cov = want_cov ? p->covariance : nullptr;
     a.flag = dflag;
-    a.scratch = scratch;
-    a.scratch_per_cta = per_cta;
+    a.scratch = (T*)scratch;
+    a.scratch_per_cta = per_cta * (int64_t)(sizeof(double) / sizeof(T));
+    a.baseR = baseR;
   };
   auto grid = [&](int64_t items) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(items, ncta)); };
+  const ctak::RawA raw{p->H, p->F, p->c, p->K, p->G, p->o, p->C, p->K_type, p->C_type, p->obs_rows, p->mmax};
   {
-    ctak::CArgs a;
+    ctak::CArgs<T> a;
     common(a, 0);
     a.ce = eq_level(0);
-    const ctak::RawA raw{p->H, p->F, p->c, p->K, p->G, p->o, p->C, p->K_type, p->C_type, p->obs_rows, p->mmax};
-    UKG_LAUNCH(UKG_K_WEIGH, st, (ctak::weigh_cta<<<grid(p->nsteps), cta::NT, 0, st>>>(a, raw, p->nsteps)));
+    UKG_LAUNCH(UKG_K_WEIGH, st, (ctak::weigh_cta<T><<<grid(p->nsteps), cta::NT, 0, st>>>(a, raw, p->nsteps)));
   }
+  const int kPair = P.fp32 ? UKG_K_PAIR32 : UKG_K_PAIR, kSolve = P.fp32 ? UKG_K_SOLVE32 : UKG_K_SOLVE;
   for (int l = 0; l < nlev; ++l) {
-    ctak::CArgs a;
+    ctak::CArgs<T> a;
     common(a, l);
     a.ce = eq_level(l);
     if (l + 1 < nlev) a.ne = eq_level(l + 1);
-    if (lp[l].npairs > 0) UKG_LAUNCH(UKG_K_PAIR, st, (ctak::pair_cta<<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
-    if (lp[l].ntail > 0) UKG_LAUNCH(UKG_K_TAIL, st, (ctak::tail_cta<<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
+    if (lp[l].npairs > 0) UKG_LAUNCH(kPair, st, (ctak::pair_cta<T><<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
+    if (lp[l].ntail > 0) UKG_LAUNCH(UKG_K_TAIL, st, (ctak::tail_cta<T><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
   }
   for (int l = nlev - 2; l >= 0; --l) {
-    ctak::CArgs a;
+    ctak::CArgs<T> a;
     common(a, l);
     if (lp[l].nsolve > 0)
-      UKG_LAUNCH(UKG_K_SOLVE, st,
-                 (ctak::solve_cta<<<grid(lp[l].nsolve), cta::NT, 0, st>>>(a, want_cov ? 1 : 0)));
+      UKG_LAUNCH(kSolve, st, (ctak::solve_cta<T><<<grid(lp[l].nsolve), cta::NT, 0, st>>>(a, want_cov ? 1 : 0)));
+  }
+  /* ---- refinement sweeps (FP32 factors): FP64 residual, transpose solves, solves ---- */
+  if constexpr (sizeof(T) == sizeof(float)) {
+    const int requested = (int)((options >> 21) & 3u);
+    const int sweeps = P.refine ? (requested ? requested : 2) : 0;
+    double* dx = P.refine ? (double*)(B + P.o_dx) : nullptr;
+    auto pargs = [&](int l) { /* for rt_base_kernel and atr_kernel (no level arrays) */
+      Args<float, float> a;
+      memset(&a, 0, sizeof(a));
+      a.ct = tables(l);
+      a.nt = tables(l + 1);
+      a.n = n;
+      a.mx = mx;
+      a.level = l;
+      a.ntracks = T_;
+      a.track_start = dtab + P.off_ts;
+      a.state = dx;
+      a.flag = dflag;
+      a.baseR = baseR;
+      return a;
+    };
+    const RawDev rawd{p->H, p->F, p->c, p->K, p->G, p->o, p->C, p->K_type, p->C_type, p->obs_rows, p->mmax};
+    for (int sw = 0; sw < sweeps; ++sw) {
+      Soa<double> wE{(double*)(B + P.o_rE), P.S0}, zp{(double*)(B + P.o_rO), P.S0};
+      Soa<float> z0{(float*)(B + P.o_z[0]), std::max<int64_t>(lp[0].S, 1)};
+      {
+        ctak::CArgs<float> a;
+        common(a, 0);
+        a.ce = eq_level(0);
+        UKG_LAUNCH(UKG_K_RESID, st,
+                   (ctak::residual_cta<<<grid(p->nsteps), cta::NT, 0, st>>>(a, raw, wE, zp, (double*)scratch, per_cta,
+                                                                           p->nsteps)));
+        Args<float, float> r = pargs(0);
+        r.state = p->state;
+        UKG_LAUNCH(UKG_K_RESID, st,
+                   (atr_kernel<<<(unsigned)((p->nsteps + 127) / 128), 128, 0, st>>>(r, rawd, wE, zp, z0, p->nsteps)));
+      }
+      for (int l = 0; l < nlev; ++l) {
+        Args<float, float> a = pargs(l);
+        ctak::CArgs<float> ca;
+        common(ca, l);
+        Soa<float> zc{(float*)(B + P.o_z[l]), std::max<int64_t>(lp[l].S, 1)};
+        Soa<float> yc{(float*)(B + P.o_y[l]), std::max<int64_t>(lp[l].E, 1)};
+        if (lp[l].nsolve > 0)
+          UKG_LAUNCH(UKG_K_RT, st,
+                     (ctak::rt_even_aos<<<(unsigned)((lp[l].nsolve + 127) / 128), 128, 0, st>>>(ca, zc, yc)));
+        if (lp[l].npairs > 0 && l + 1 < nlev) {
+          Soa<float> zn{(float*)(B + P.o_z[l + 1]), std::max<int64_t>(lp[l + 1].S, 1)};
+          UKG_LAUNCH(UKG_K_RT, st,
+                     (ctak::rt_odd_aos<<<(unsigned)((lp[l].npairs + 127) / 128), 128, 0, st>>>(ca, zc, yc, zn)));
+        }
+        if (lp[l].ntail > 0) {
+          Soa<float> tmp{(float*)(B + P.o_tmp), std::max(T_, 1)};
+          UKG_LAUNCH(UKG_K_RT, st, (rt_base_kernel<<<(unsigned)((lp[l].ntail + 127) / 128), 128, 0, st>>>(a, zc, tmp)));
+        }
+      }
+      for (int l = nlev - 2; l >= 0; --l) {
+        ctak::CArgs<float> a;
+        common(a, l);
+        a.state = dx;
+        a.cov = nullptr;
+        a.yrhs = Soa<float>{(float*)(B + P.o_y[l]), std::max<int64_t>(lp[l].E, 1)};
+        if (lp[l].nsolve > 0)
+          UKG_LAUNCH(UKG_K_RSOLVE, st, (ctak::solve_cta<float><<<grid(lp[l].nsolve), cta::NT, 0, st>>>(a, 0)));
+      }
+      const int64_t cnt = p->nsteps * n;
+      UKG_LAUNCH(UKG_K_REFINE, st, (add_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, st>>>(p->state, dx, cnt)));
+    }
   }
   if (enqueue_only) return 0;
   int hflag = 0;
@@ -2996,22 +3069,26 @@ extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* 
   if (p->nsteps == 0) return 0;
   const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
   const int mxp = p->mmax > p->n ? p->mmax : p->n;
-  if (p->n >= kCtaMinN || mxp > 8) { /* larger shapes: CTA kernels, FP64 (also for FP32_REFINE requests) */
+  if (p->n >= kCtaMinN || mxp > 8) { /* larger shapes: CTA kernels (FP64, or FP32 + refinement) */
     if (mxp > kCtaMaxN)
       return ukg_set_error(KALMAN_GPU_EINVAL, "state dimension %d (observation rows %d) above this build's limit %d",
                            p->n, p->mmax, kCtaMaxN);
+    const bool f32 = (options & KALMAN_GPU_FP32_REFINE) != 0;
     Plan P;
-    const size_t need = build_plan(p, want_cov, false, false, P, nullptr, 0);
+    const size_t need = build_plan(p, want_cov, f32, f32, P, nullptr, 0);
     if (need == 0) return ukg_set_error(KALMAN_GPU_EINVAL, "tracks longer than 2^%d steps", kMaxLevels - 1);
     if (int e = ensure_mapped_tables(need)) return e;
-    build_plan(p, want_cov, false, false, P, tl_mtab.host, need);
+    build_plan(p, want_cov, f32, f32, P, tl_mtab.host, need);
     const int ncta = cta_count();
     const int64_t per = cta_scratch_per_cta(p->n, p->mmax);
     const size_t scratch_off = align_up(P.bytes, 256);
     void* base = nullptr;
     if (int e = ensure_workspace(scratch_off + (size_t)ncta * per * sizeof(double), &base)) return e;
-    return run_plan_cta(options, p, (cudaStream_t)cuda_stream, P, tl_mtab.dev, (char*)base,
-                        (double*)((char*)base + scratch_off), per, ncta);
+    if (f32)
+      return run_plan_cta<float>(options, p, (cudaStream_t)cuda_stream, P, tl_mtab.dev, (char*)base,
+                                 (char*)base + scratch_off, per, ncta);
+    return run_plan_cta<double>(options, p, (cudaStream_t)cuda_stream, P, tl_mtab.dev, (char*)base,
+                                (char*)base + scratch_off, per, ncta);
   }
   const bool fp32 = (options & KALMAN_GPU_FP32_REFINE) != 0;
   Plan P;
@@ -3164,7 +3241,7 @@ extern "C" kalman_gpu_plan_t* kalman_gpu_plan_create(uint32_t options, const kal
                   p->mmax, kCtaMaxN);
     return nullptr;
   }
-  const bool fp32 = !cta && (options & KALMAN_GPU_FP32_REFINE) != 0;
+  const bool fp32 = (options & KALMAN_GPU_FP32_REFINE) != 0;
   Plan P;
   const size_t need = build_plan(p, want_cov, fp32, fp32, P, nullptr, 0);
   if (need == 0) {
@@ -3196,9 +3273,12 @@ extern "C" kalman_gpu_plan_t* kalman_gpu_plan_create(uint32_t options, const kal
   if (e == cudaSuccess) {
     const int prof = ukg_prof_pause(); /* no profiling events inside the graph */
     int st;
-    if (cta)
-      st = run_plan_cta(options, p, cs, P, nullptr, (char*)pl->work, (double*)((char*)pl->work + scratch_off), per,
-                        ncta, true);
+    if (cta && fp32)
+      st = run_plan_cta<float>(options, p, cs, P, nullptr, (char*)pl->work, (char*)pl->work + scratch_off, per, ncta,
+                               true);
+    else if (cta)
+      st = run_plan_cta<double>(options, p, cs, P, nullptr, (char*)pl->work, (char*)pl->work + scratch_off, per, ncta,
+                                true);
     else if (fp32)
       st = run_plan<float>(options, p, cs, P, nullptr, (char*)pl->work, nullptr, true);
     else

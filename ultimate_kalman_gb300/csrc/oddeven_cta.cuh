@@ -34,17 +34,22 @@ struct RecA {
   Aos<T> R, Ft, Y, rhs, U;
 };
 
+/* T: the arithmetic type of the levels and records (FP64, or FP32 in the
+ * precision form); states and covariances are FP64 */
+template <typename T>
 struct CArgs {
   Tables ct, nt;
-  EqA<double> ce, ne;
-  RecA<double> cr, nr;
+  EqA<T> ce, ne;
+  RecA<T> cr, nr;
   int n, mx, level, ntracks;
   const int64_t* track_start;
-  double* state;
+  double* state;   /* x, or the correction d in a refinement sweep */
   double* cov;
   int* flag;
-  double* scratch; /* per CTA: scratch + blockIdx.x * scratch_per_cta */
+  T* scratch;      /* per CTA: scratch + blockIdx.x * scratch_per_cta */
   int64_t scratch_per_cta;
+  Soa<T> baseR;    /* refinement: base-case R per track (p may be null) */
+  Soa<T> yrhs;     /* refinement: right-hand side of the even steps (p may be null) */
 };
 
 struct RawA {
@@ -59,14 +64,15 @@ struct RawA {
  * factor, panel [G | o] (m x (n+1)) by C's; written slot-major to level 0.
  * Scratch: n^2 (L) + n (2n+1) (panel) + rows x NT (the 'W' product).
  * ------------------------------------------------------------------------ */
-__global__ void __launch_bounds__(NT) weigh_cta(CArgs a, RawA raw, int64_t nsteps)
+template <typename T>
+__global__ void __launch_bounds__(NT) weigh_cta(CArgs<T> a, RawA raw, int64_t nsteps)
 {
-  __shared__ double red[33];
+  __shared__ T red[33];
   const int n = a.n, mx = a.mx, mm = raw.mmax, tid = threadIdx.x;
   const int rmax = n > mm ? n : mm;
-  double* L = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
-  double* B = L + (int64_t)rmax * rmax;
-  double* tmp = B + (int64_t)rmax * (2 * n + 1);
+  T* L = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
+  T* B = L + (int64_t)rmax * rmax;
+  T* tmp = B + (int64_t)rmax * (2 * n + 1);
   const int64_t nn = (int64_t)n * n;
   for (int64_t g = blockIdx.x; g < nsteps; g += gridDim.x) {
     const int t = find_track(a.track_start, a.ntracks, g);
@@ -76,10 +82,10 @@ __global__ void __launch_bounds__(NT) weigh_cta(CArgs a, RawA raw, int64_t nstep
       const int ld = 2 * n + 1;
       for (int e = tid; e < n * ld; e += NT) {
         const int r = e / ld, c = e - r * ld;
-        double v;
-        if (c < n) v = raw.H[g * nn + (int64_t)c * n + r];
-        else if (c < 2 * n) v = -raw.F[g * nn + (int64_t)(c - n) * n + r];
-        else v = raw.c[g * n + r];
+        T v;
+        if (c < n) v = ukg_df::narrow<T>(raw.H[g * nn + (int64_t)c * n + r]);
+        else if (c < 2 * n) v = -ukg_df::narrow<T>(raw.F[g * nn + (int64_t)(c - n) * n + r]);
+        else v = ukg_df::narrow<T>(raw.c[g * n + r]);
         B[e] = v;
       }
       __syncthreads();
@@ -104,7 +110,7 @@ __global__ void __launch_bounds__(NT) weigh_cta(CArgs a, RawA raw, int64_t nstep
       const int ld = n + 1;
       for (int e = tid; e < m * ld; e += NT) {
         const int r = e / ld, c = e - r * ld;
-        B[e] = c < n ? raw.G[g * (int64_t)mm * n + (int64_t)c * mm + r] : raw.o[g * mm + r];
+        B[e] = ukg_df::narrow<T>(c < n ? raw.G[g * (int64_t)mm * n + (int64_t)c * mm + r] : raw.o[g * mm + r]);
       }
       __syncthreads();
       const char ct = raw.C_type[g];
@@ -125,14 +131,15 @@ __global__ void __launch_bounds__(NT) weigh_cta(CArgs a, RawA raw, int64_t nstep
  * forward elimination of one pair per CTA: stages A, C, B
  * Scratch: the largest panel, 2n x (3n+1).
  * ------------------------------------------------------------------------ */
-__global__ void __launch_bounds__(NT) pair_cta(CArgs a)
+template <typename T>
+__global__ void __launch_bounds__(NT) pair_cta(CArgs<T> a)
 {
-  __shared__ double red[33];
+  __shared__ T red[33];
   const int n = a.n, mx = a.mx, tid = threadIdx.x;
-  double* A = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
-  const EqA<double>& C = a.ce;
-  const EqA<double>& Nx = a.ne;
-  const RecA<double>& Rr = a.cr;
+  T* A = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
+  const EqA<T>& C = a.ce;
+  const EqA<T>& Nx = a.ne;
+  const RecA<T>& Rr = a.cr;
   for (int64_t item = blockIdx.x; item < a.ct.npairs; item += gridDim.x) {
     const int t = find_track(a.ct.pair, a.ntracks, item);
     const int64_t p = item - a.ct.pair[t];
@@ -145,8 +152,8 @@ __global__ void __launch_bounds__(NT) pair_cta(CArgs a)
       const int rows = mj + n, ld = 2 * n + 1;
       for (int e = tid; e < rows * ld; e += NT) {
         const int r = e / ld, c = e - r * ld;
-        double v;
-        if (r < mj) v = c < n ? C.G.at(c * mx + r, sj) : c == n ? C.o.at(r, sj) : 0.0;
+        T v;
+        if (r < mj) v = c < n ? C.G.at(c * mx + r, sj) : c == n ? C.o.at(r, sj) : T(0);
         else {
           const int rr = r - mj;
           v = c < n ? C.F.at(c * n + rr, sj1) : c == n ? C.c.at(rr, sj1) : C.H.at((c - n - 1) * n + rr, sj1);
@@ -157,7 +164,7 @@ __global__ void __launch_bounds__(NT) pair_cta(CArgs a)
       ::cta::householder(A, ld, rows, n, ld, red);
       for (int e = tid; e < n * n; e += NT) {
         const int r = e / n, c = e - r * n; /* R~ (r, c), Y~ (r, c) */
-        Rr.R.at(c * n + r, se) = r <= c ? A[(int64_t)r * ld + c] : 0.0;
+        Rr.R.at(c * n + r, se) = r <= c ? A[(int64_t)r * ld + c] : T(0);
         Rr.Y.at(c * n + r, se) = A[(int64_t)r * ld + n + 1 + c];
       }
       for (int r = tid; r < n; r += NT) Rr.rhs.at(r, se) = A[(int64_t)r * ld + n];
@@ -183,7 +190,7 @@ __global__ void __launch_bounds__(NT) pair_cta(CArgs a)
       const int g2 = rows < n ? rows : n;
       for (int e = tid; e < g2 * n; e += NT) {
         const int r = e / n, c = e - r * n;
-        Nx.G.at(c * mx + r, sn) = r <= c ? A[(int64_t)r * ld + c] : 0.0;
+        Nx.G.at(c * mx + r, sn) = r <= c ? A[(int64_t)r * ld + c] : T(0);
       }
       for (int r = tid; r < g2; r += NT) Nx.o.at(r, sn) = A[(int64_t)r * ld + n];
       if (tid == 0) Nx.m[sn] = g2;
@@ -191,7 +198,7 @@ __global__ void __launch_bounds__(NT) pair_cta(CArgs a)
     }
     /* stage B: [H_j | F_j | c_j | 0; R~ | 0 | rhs~ | Y~] */
     if (p == 0) {
-      for (int e = tid; e < n * n; e += NT) Rr.Ft.at(e, se) = 0.0;
+      for (int e = tid; e < n * n; e += NT) Rr.Ft.at(e, se) = T(0);
       __syncthreads();
       continue;
     }
@@ -199,13 +206,13 @@ __global__ void __launch_bounds__(NT) pair_cta(CArgs a)
       const int rows = 2 * n, ld = 3 * n + 1;
       for (int e = tid; e < rows * ld; e += NT) {
         const int r = e / ld, c = e - r * ld;
-        double v;
+        T v;
         if (r < n) {
-          v = c < n ? C.H.at(c * n + r, sj) : c < 2 * n ? C.F.at((c - n) * n + r, sj) : c == 2 * n ? C.c.at(r, sj) : 0.0;
+          v = c < n ? C.H.at(c * n + r, sj) : c < 2 * n ? C.F.at((c - n) * n + r, sj) : c == 2 * n ? C.c.at(r, sj) : T(0);
         } else {
           const int rr = r - n;
-          v = c < n ? (rr <= c ? Rr.R.at(c * n + rr, se) : 0.0)
-              : c < 2 * n ? 0.0 : c == 2 * n ? Rr.rhs.at(rr, se) : Rr.Y.at((c - 2 * n - 1) * n + rr, se);
+          v = c < n ? (rr <= c ? Rr.R.at(c * n + rr, se) : T(0))
+              : c < 2 * n ? T(0) : c == 2 * n ? Rr.rhs.at(rr, se) : Rr.Y.at((c - 2 * n - 1) * n + rr, se);
         }
         A[e] = v;
       }
@@ -213,7 +220,7 @@ __global__ void __launch_bounds__(NT) pair_cta(CArgs a)
       ::cta::householder(A, ld, rows, n, ld, red);
       for (int e = tid; e < n * n; e += NT) {
         const int r = e / n, c = e - r * n;
-        Rr.R.at(c * n + r, se) = r <= c ? A[(int64_t)r * ld + c] : 0.0;
+        Rr.R.at(c * n + r, se) = r <= c ? A[(int64_t)r * ld + c] : T(0);
         Rr.Ft.at(c * n + r, se) = A[(int64_t)r * ld + n + c];
         Nx.F.at(c * n + r, sn) = A[(int64_t)(n + r) * ld + n + c];
         Rr.Y.at(c * n + r, se) = A[(int64_t)r * ld + 2 * n + 1 + c];
@@ -232,14 +239,15 @@ __global__ void __launch_bounds__(NT) pair_cta(CArgs a)
  * odd-length tracks: the single last step and its fix-up, or the base case.
  * Scratch: the (n+m) x (2n+1) panel, an n x n inverse, an n-vector.
  * ------------------------------------------------------------------------ */
-__global__ void __launch_bounds__(NT) tail_cta(CArgs a)
+template <typename T>
+__global__ void __launch_bounds__(NT) tail_cta(CArgs<T> a)
 {
-  __shared__ double red[33];
+  __shared__ T red[33];
   const int n = a.n, mx = a.mx, tid = threadIdx.x;
-  double* A = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
-  const EqA<double>& C = a.ce;
-  const EqA<double>& Nx = a.ne;
-  const RecA<double>& Rr = a.cr;
+  T* A = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
+  const EqA<T>& C = a.ce;
+  const EqA<T>& Nx = a.ne;
+  const RecA<T>& Rr = a.cr;
   for (int64_t item = blockIdx.x; item < a.ct.ntail; item += gridDim.x) {
     const int t = (int)a.ct.tail[item];
     const int64_t L = a.ct.L[t], sb = a.ct.slot[t];
@@ -265,20 +273,25 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs a)
       ::cta::householder(A, ld, m0, n, ld, red);
       if (tid == 0)
         for (int i = 0; i < n; ++i)
-          if (A[(int64_t)i * ld + i] == 0.0) atomicOr(a.flag, 2);
-      double* v = A + (int64_t)m0 * ld; /* the right-hand side, then x */
+          if (A[(int64_t)i * ld + i] == T(0)) atomicOr(a.flag, 2);
+      if (a.baseR.p) /* the base factor, for the refinement's transpose solve */
+        for (int e = tid; e < n * n; e += NT) {
+          const int r = e % n, c = e / n;
+          a.baseR.at(c * n + r, t) = r <= c ? A[(int64_t)r * ld + c] : T(0);
+        }
+      T* v = A + (int64_t)m0 * ld; /* the right-hand side, then x */
       for (int i = tid; i < n; i += NT) v[i] = A[(int64_t)i * ld + n];
       __syncthreads();
       solve_upper_vec(A, ld, n, v);
-      for (int i = tid; i < n; i += NT) x[i] = v[i];
+      for (int i = tid; i < n; i += NT) x[i] = ukg_df::widen(v[i]);
       if (S) {
-        double* Ri = v + n; /* R^{-1}, row-major n x n */
-        for (int e = tid; e < n * n; e += NT) Ri[e] = (e / n == e % n) ? 1.0 : 0.0;
+        T* Ri = v + n; /* R^{-1}, row-major n x n */
+        for (int e = tid; e < n * n; e += NT) Ri[e] = (e / n == e % n) ? T(1) : T(0);
         __syncthreads();
         solve_upper_cols(A, ld, n, Ri, n, 0, n);
         for (int e = tid; e < n * n; e += NT) { /* S(r, c) = sum_k Ri(r, k) Ri(c, k) */
           const int r = e / n, c = e - r * n;
-          double s = 0.0;
+          T s = T(0);
           for (int k = (r > c ? r : c); k < n; ++k) s = fma(Ri[(int64_t)r * n + k], Ri[(int64_t)c * n + k], s);
           S[(int64_t)c * n + r] = s;
         }
@@ -294,8 +307,8 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs a)
     /* stage A on [G_s | o_s]: its R~ and o' go into the lower rows of the
        stage-B panel, built in the same scratch below it */
     const int ldA = n + 1, ldT = 2 * n + 1, rowsT = n + mt;
-    double* WS = A;
-    double* WT = A + (int64_t)(ms > 0 ? ms : 1) * ldA;
+    T* WS = A;
+    T* WT = A + (int64_t)(ms > 0 ? ms : 1) * ldA;
     if (ms > 0) {
       for (int e = tid; e < ms * ldA; e += NT) {
         const int r = e / ldA, c = e - r * ldA;
@@ -306,11 +319,11 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs a)
     }
     for (int e = tid; e < rowsT * ldT; e += NT) {
       const int r = e / ldT, c = e - r * ldT;
-      double v;
+      T v;
       if (r < n) v = c < n ? C.H.at(c * n + r, s) : c < 2 * n ? C.F.at((c - n) * n + r, s) : C.c.at(r, s);
       else {
         const int rr = r - n;
-        v = c < n ? (rr <= c ? WS[(int64_t)rr * ldA + c] : 0.0) : c < 2 * n ? 0.0 : WS[(int64_t)rr * ldA + n];
+        v = c < n ? (rr <= c ? WS[(int64_t)rr * ldA + c] : T(0)) : c < 2 * n ? T(0) : WS[(int64_t)rr * ldA + n];
       }
       WT[e] = v;
     }
@@ -318,9 +331,9 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs a)
     ::cta::householder(WT, ldT, rowsT, n, ldT, red);
     for (int e = tid; e < n * n; e += NT) {
       const int r = e / n, c = e - r * n;
-      Rr.R.at(c * n + r, es) = r <= c ? WT[(int64_t)r * ldT + c] : 0.0;
+      Rr.R.at(c * n + r, es) = r <= c ? WT[(int64_t)r * ldT + c] : T(0);
       Rr.Ft.at(c * n + r, es) = WT[(int64_t)r * ldT + n + c];
-      Rr.Y.at(c * n + r, es) = 0.0;
+      Rr.Y.at(c * n + r, es) = T(0);
     }
     for (int r = tid; r < n; r += NT) Rr.rhs.at(r, es) = WT[(int64_t)r * ldT + 2 * n];
     __syncthreads();
@@ -331,7 +344,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs a)
       __syncthreads();
       continue;
     }
-    double* WF = WT + (int64_t)rowsT * ldT;
+    T* WF = WT + (int64_t)rowsT * ldT;
     const int ldF = n + 1;
     for (int e = tid; e < rF * ldF; e += NT) {
       const int r = e / ldF, c = e - r * ldF;
@@ -343,7 +356,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs a)
     const int g2 = rF < n ? rF : n;
     for (int e = tid; e < g2 * n; e += NT) {
       const int r = e / n, c = e - r * n;
-      Nx.G.at(c * mx + r, sn) = r <= c ? WF[(int64_t)r * ldF + c] : 0.0;
+      Nx.G.at(c * mx + r, sn) = r <= c ? WF[(int64_t)r * ldF + c] : T(0);
     }
     for (int r = tid; r < g2; r += NT) Nx.o.at(r, sn) = WF[(int64_t)r * ldF + n];
     if (tid == 0) Nx.m[sn] = g2;
@@ -359,17 +372,18 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs a)
  *   S_j = R^{-1} (I + W B^T) R^{-T}
  * Scratch (row-major): R, B (n x 2n), W (n x 2n), M, X (n x n each), x.
  * ------------------------------------------------------------------------ */
-__global__ void __launch_bounds__(NT) solve_cta(CArgs a, int want_cov)
+template <typename T>
+__global__ void __launch_bounds__(NT) solve_cta(CArgs<T> a, int want_cov)
 {
   const int n = a.n, tid = threadIdx.x;
   const int64_t nn = (int64_t)n * n;
-  double* R = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
-  double* Bm = R + nn;       /* n x 2n */
-  double* W = Bm + 2 * nn;   /* n x 2n */
-  double* M = W + 2 * nn;    /* n x n */
-  double* X = M + nn;        /* n x n */
-  double* xv = X + nn;       /* n */
-  const RecA<double>& Rr = a.cr;
+  T* R = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
+  T* Bm = R + nn;       /* n x 2n */
+  T* W = Bm + 2 * nn;   /* n x 2n */
+  T* M = W + 2 * nn;    /* n x n */
+  T* X = M + nn;        /* n x n */
+  T* xv = X + nn;       /* n */
+  const RecA<T>& Rr = a.cr;
   for (int64_t item = blockIdx.x; item < a.ct.nsolve; item += gridDim.x) {
     const int t = find_track(a.ct.solve, a.ntracks, item);
     const int64_t j = 2 * (item - a.ct.solve[t]), L = a.ct.L[t];
@@ -380,25 +394,25 @@ __global__ void __launch_bounds__(NT) solve_cta(CArgs a, int want_cov)
     for (int e = tid; e < n * n; e += NT) {
       const int r = e / n, c = e - r * n;
       R[e] = Rr.R.at(c * n + r, item);
-      Bm[(int64_t)r * 2 * n + c] = hp ? Rr.Ft.at(c * n + r, item) : 0.0;
-      Bm[(int64_t)r * 2 * n + n + c] = hn ? Rr.Y.at(c * n + r, item) : 0.0;
+      Bm[(int64_t)r * 2 * n + c] = hp ? Rr.Ft.at(c * n + r, item) : T(0);
+      Bm[(int64_t)r * 2 * n + n + c] = hn ? Rr.Y.at(c * n + r, item) : T(0);
     }
     __syncthreads();
     /* state */
     for (int r = tid; r < n; r += NT) {
-      double s = Rr.rhs.at(r, item);
+      T s = a.yrhs.p ? a.yrhs.at(r, item) : Rr.rhs.at(r, item);
       if (hp)
-        for (int k = 0; k < n; ++k) s = fma(-Bm[(int64_t)r * 2 * n + k], a.state[om * n + k], s);
+        for (int k = 0; k < n; ++k) s = fma(-Bm[(int64_t)r * 2 * n + k], ukg_df::narrow<T>(a.state[om * n + k]), s);
       if (hn)
-        for (int k = 0; k < n; ++k) s = fma(-Bm[(int64_t)r * 2 * n + n + k], a.state[op * n + k], s);
+        for (int k = 0; k < n; ++k) s = fma(-Bm[(int64_t)r * 2 * n + n + k], ukg_df::narrow<T>(a.state[op * n + k]), s);
       xv[r] = s;
     }
     __syncthreads();
     solve_upper_vec(R, n, n, xv);
-    for (int r = tid; r < n; r += NT) a.state[oj * n + r] = xv[r];
+    for (int r = tid; r < n; r += NT) a.state[oj * n + r] = ukg_df::widen(xv[r]);
     if (tid == 0)
       for (int i = 0; i < n; ++i)
-        if (R[(int64_t)i * n + i] == 0.0) atomicOr(a.flag, 2);
+        if (R[(int64_t)i * n + i] == T(0)) atomicOr(a.flag, 2);
     if (!want_cov) {
       __syncthreads();
       continue;
@@ -407,29 +421,29 @@ __global__ void __launch_bounds__(NT) solve_cta(CArgs a, int want_cov)
     const double* Smm = hp ? a.cov + om * nn : nullptr;
     const double* Spp = hn ? a.cov + op * nn : nullptr;
     const int64_t smp = (hp && hn) ? a.nt.slot[t] + (j + 1) / 2 : 0;
-    auto sigma = [&](int k, int q) -> double { /* Sigma(k, q), 0 <= k, q < 2n */
+    auto sigma = [&](int k, int q) -> T { /* Sigma(k, q), 0 <= k, q < 2n */
       if (k < n) {
-        if (q < n) return hp ? Smm[(int64_t)q * n + k] : 0.0;
-        return (hp && hn) ? a.nr.U.at((q - n) * n + k, smp) : 0.0; /* Smp(k, q-n) */
+        if (q < n) return hp ? Smm[(int64_t)q * n + k] : T(0);
+        return (hp && hn) ? a.nr.U.at((q - n) * n + k, smp) : T(0); /* Smp(k, q-n) */
       }
-      if (q < n) return (hp && hn) ? a.nr.U.at((k - n) * n + q, smp) : 0.0; /* Smp(q, k-n) */
-      return hn ? Spp[(int64_t)(q - n) * n + (k - n)] : 0.0;
+      if (q < n) return (hp && hn) ? a.nr.U.at((k - n) * n + q, smp) : T(0); /* Smp(q, k-n) */
+      return hn ? Spp[(int64_t)(q - n) * n + (k - n)] : T(0);
     };
     const int k0 = hp ? 0 : n, k1 = hn ? 2 * n : n;
     for (int r = tid; r < n; r += NT)
       for (int q = k0; q < k1; ++q) {
-        double s = 0.0;
+        T s = T(0);
         for (int k = k0; k < k1; ++k) s = fma(Bm[(int64_t)r * 2 * n + k], sigma(k, q), s);
         W[(int64_t)r * 2 * n + q] = s;
       }
     for (int r = tid; r < n; r += NT)
       for (int q = 0; q < 2 * n; ++q)
-        if (q < k0 || q >= k1) W[(int64_t)r * 2 * n + q] = 0.0;
+        if (q < k0 || q >= k1) W[(int64_t)r * 2 * n + q] = T(0);
     __syncthreads();
     /* M = I + W B^T */
     for (int e = tid; e < n * n; e += NT) {
       const int r = e / n, c = e - r * n;
-      double s = r == c ? 1.0 : 0.0;
+      T s = r == c ? T(1) : T(0);
       for (int q = k0; q < k1; ++q) s = fma(W[(int64_t)r * 2 * n + q], Bm[(int64_t)c * 2 * n + q], s);
       M[e] = s;
     }
@@ -458,6 +472,169 @@ __global__ void __launch_bounds__(NT) solve_cta(CArgs a, int want_cov)
       So[(int64_t)c * n + r] = X[e];
     }
     __syncthreads();
+  }
+}
+
+/* ---------------------------------------------------------------------------
+ * refinement right-hand side, first part, one step per CTA (FP64, from the
+ * raw equations; as residual_kernel): with r = c + F x_{i-1} - H x_i and
+ * s = o - G x_i,  wE = K^{-1} r,  zp = H^T wE + G^T C^{-1} s.  Scratch: a
+ * factor (rmax^2) and four vectors of rmax.
+ * ------------------------------------------------------------------------ */
+/* w <- Cov^{-1} w for the covariance factor (cov column-major, ld ldc, rows
+ * x rows): 'C' L^{-T} L^{-1} (L = chol), 'U'/'F' the same with L = tril(cov),
+ * 'W' W^T W, 'w' diag(cov)^2.  w and tmp are vectors shared by the CTA. */
+__device__ void apply_precision_cta(char type, const double* cov, int ldc, int rows, double* L, double* w, double* tmp)
+{
+  const int tid = threadIdx.x;
+  if (type == 'w') {
+    for (int i = tid; i < rows; i += NT) w[i] *= cov[i] * cov[i];
+    __syncthreads();
+    return;
+  }
+  if (type == 'W') {
+    for (int i = tid; i < rows; i += NT) {
+      double sm = 0.0;
+      for (int j = 0; j < rows; ++j) sm = fma(cov[(int64_t)j * ldc + i], w[j], sm);
+      tmp[i] = sm;
+    }
+    __syncthreads();
+    for (int j = tid; j < rows; j += NT) {
+      double sm = 0.0;
+      for (int i = 0; i < rows; ++i) sm = fma(cov[(int64_t)j * ldc + i], tmp[i], sm);
+      w[j] = sm;
+    }
+    __syncthreads();
+    return;
+  }
+  if (type != 'C' && type != 'U' && type != 'F') return;
+  for (int e = tid; e < rows * rows; e += NT) {
+    const int i = e / rows, j = e - i * rows;
+    L[e] = i >= j ? cov[(int64_t)j * ldc + i] : 0.0;
+  }
+  __syncthreads();
+  if (type == 'C')
+    for (int j = 0; j < rows; ++j) {
+      if (tid == 0) {
+        const double d = L[(int64_t)j * rows + j];
+        L[(int64_t)j * rows + j] = d > 0.0 ? sqrt(d) : 1.0; /* the weighing reports a bad factor */
+      }
+      __syncthreads();
+      const double ljj = L[(int64_t)j * rows + j];
+      for (int i = j + 1 + tid; i < rows; i += NT) L[(int64_t)i * rows + j] /= ljj;
+      __syncthreads();
+      for (int i = j + 1 + tid; i < rows; i += NT) {
+        const double lij = L[(int64_t)i * rows + j];
+        for (int l = j + 1; l <= i; ++l) L[(int64_t)i * rows + l] = fma(-lij, L[(int64_t)l * rows + j], L[(int64_t)i * rows + l]);
+      }
+      __syncthreads();
+    }
+  for (int j = 0; j < rows; ++j) { /* L^{-1} w */
+    if (tid == 0) w[j] /= L[(int64_t)j * rows + j];
+    __syncthreads();
+    const double wj = w[j];
+    for (int i = j + 1 + tid; i < rows; i += NT) w[i] = fma(-L[(int64_t)i * rows + j], wj, w[i]);
+    __syncthreads();
+  }
+  for (int j = rows - 1; j >= 0; --j) { /* L^{-T} w */
+    if (tid == 0) w[j] /= L[(int64_t)j * rows + j];
+    __syncthreads();
+    const double wj = w[j];
+    for (int i = tid; i < j; i += NT) w[i] = fma(-L[(int64_t)j * rows + i], wj, w[i]);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(NT) residual_cta(CArgs<float> a, RawA raw, Soa<double> wE, Soa<double> zp,
+                                                   double* scratch, int64_t per_cta, int64_t nsteps)
+{
+  const int n = a.n, mm = raw.mmax, tid = threadIdx.x;
+  const int rmax = n > mm ? n : mm;
+  const int64_t nn = (int64_t)n * n;
+  double* L = scratch + (int64_t)blockIdx.x * per_cta;
+  double* w = L + (int64_t)rmax * rmax;
+  double* tmp = w + rmax;
+  double* z = tmp + rmax;
+  for (int64_t g = blockIdx.x; g < nsteps; g += gridDim.x) {
+    const int t = find_track(a.track_start, a.ntracks, g);
+    const int64_t i = g - a.track_start[t], q = a.ct.slot[t] + i;
+    const double* x = a.state + g * n;
+    for (int c = tid; c < n; c += NT) z[c] = 0.0;
+    if (i > 0) {
+      const double* xm = x - n;
+      const double* H = raw.H + g * nn;
+      const double* F = raw.F + g * nn;
+      for (int r = tid; r < n; r += NT) {
+        double sm = raw.c[g * n + r];
+        for (int c = 0; c < n; ++c) sm = fma(F[(int64_t)c * n + r], xm[c], fma(-H[(int64_t)c * n + r], x[c], sm));
+        w[r] = sm;
+      }
+      __syncthreads();
+      apply_precision_cta(raw.K_type[g], raw.K + g * nn, n, n, L, w, tmp);
+      for (int r = tid; r < n; r += NT) wE.at(r, q) = w[r];
+      for (int c = tid; c < n; c += NT) {
+        double sm = 0.0;
+        for (int r = 0; r < n; ++r) sm = fma(H[(int64_t)c * n + r], w[r], sm);
+        z[c] = sm;
+      }
+      __syncthreads();
+    }
+    const int m = a.ce.m[q];
+    if (m > 0) {
+      const double* G = raw.G + g * (int64_t)mm * n;
+      for (int r = tid; r < m; r += NT) {
+        double sm = raw.o[g * mm + r];
+        for (int c = 0; c < n; ++c) sm = fma(-G[(int64_t)c * mm + r], x[c], sm);
+        w[r] = sm;
+      }
+      __syncthreads();
+      apply_precision_cta(raw.C_type[g], raw.C + g * (int64_t)mm * mm, mm, m, L, w, tmp);
+      for (int c = tid; c < n; c += NT) {
+        double sm = z[c];
+        for (int r = 0; r < m; ++r) sm = fma(G[(int64_t)c * mm + r], w[r], sm);
+        z[c] = sm;
+      }
+      __syncthreads();
+    }
+    for (int c = tid; c < n; c += NT) zp.at(c, q) = z[c];
+    __syncthreads();
+  }
+}
+
+/* refinement transpose solves over slot-major FP32 records, one thread per
+ * item (as rt_even_kernel / rt_odd_kernel):
+ *   even steps  y_j = R_j^{-T} z_j
+ *   odd steps   z' = z_{2p+1} - Y_{2p}^T y_{2p} - Ft_{2p+2}^T y_{2p+2}      */
+__global__ void rt_even_aos(CArgs<float> a, Soa<float> zc, Soa<float> yc)
+{
+  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= a.ct.nsolve) return;
+  const int n = a.n;
+  const int t = find_track(a.ct.solve, a.ntracks, item);
+  const int64_t sz = a.ct.slot[t] + 2 * (item - a.ct.solve[t]);
+  for (int i = 0; i < n; ++i) {
+    float s = zc.at(i, sz);
+    for (int k = 0; k < i; ++k) s = fmaf(-a.cr.R.at(i * n + k, item), yc.at(k, item), s);
+    yc.at(i, item) = s / a.cr.R.at(i * n + i, item);
+  }
+}
+
+__global__ void rt_odd_aos(CArgs<float> a, Soa<float> zc, Soa<float> yc, Soa<float> zn)
+{
+  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= a.ct.npairs) return;
+  const int n = a.n;
+  const int t = find_track(a.ct.pair, a.ntracks, item);
+  const int64_t p = item - a.ct.pair[t], L = a.ct.L[t];
+  const int64_t so = a.ct.slot[t] + 2 * p + 1, sn = a.nt.slot[t] + p;
+  const int64_t e0 = a.ct.solve[t] + p, e1 = e0 + 1;
+  const bool right = 2 * p + 2 <= L - 1;
+  for (int c = 0; c < n; ++c) {
+    float s = zc.at(c, so);
+    for (int r = 0; r < n; ++r) s = fmaf(-a.cr.Y.at(c * n + r, e0), yc.at(r, e0), s);
+    if (right)
+      for (int r = 0; r < n; ++r) s = fmaf(-a.cr.Ft.at(c * n + r, e1), yc.at(r, e1), s);
+    zn.at(c, sn) = s;
   }
 }
 

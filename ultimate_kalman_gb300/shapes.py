@@ -60,27 +60,37 @@ def main():
     ap.add_argument("--k", type=int, default=100000)
     ap.add_argument("--algorithm", default="associative", choices=["oddeven", "associative"])
     ap.add_argument("--no-covariance", action="store_true")
+    ap.add_argument("--fp32-refine", action="store_true", help="the precision form (odd-even; states)")
+    ap.add_argument("--sweeps", type=int, default=0)
     ap.add_argument("--repeats", type=int, default=3)
     ap.add_argument("--log-cov", action="store_true", help="covariance eigenvalues log-uniform in [1e-3, 1]")
     args = ap.parse_args()
     lo = 1e-3 if args.log_cov else 0.1
     P = synthetic_track(args.k, args.n, args.m, lo=lo, log_cov=args.log_cov,
                         rho=0.995 if args.n >= 128 else 0.99)
-    cov = not args.no_covariance
-    D = native.DeviceProblem(P, covariance=cov)
-    D.smooth(args.algorithm, covariance=cov)
+    cov = not args.no_covariance and not args.fp32_refine
+    D = native.DeviceProblem(P, covariance=True)
+    kw = dict(covariance=cov, fp32_refine=args.fp32_refine, sweeps=args.sweeps)
+    D.smooth(args.algorithm, **kw)
     torch.cuda.synchronize()
     native.profile_enable(True)
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     s.record()
     for _ in range(args.repeats):
-        D.smooth(args.algorithm, covariance=cov)
+        D.smooth(args.algorithm, **kw)
     e.record()
     torch.cuda.synchronize()
     prof = native.profile_read()
     native.profile_enable(False)
     ms = s.elapsed_time(e) / args.repeats
+    rel_err = None
+    if args.fp32_refine:  # against the plain FP64 smoothing of the same track
+        X32 = D.state.clone()
+        D.smooth(args.algorithm, covariance=False)
+        X64 = D.state
+        rel_err = float(((X32 - X64).abs().amax(dim=1) / X64.abs().amax(dim=1)).max().item())
     print(json.dumps({"algorithm": args.algorithm, "n": args.n, "m": args.m, "k": args.k, "covariance": cov,
+                      "fp32_refine": args.fp32_refine, "rel_err_vs_fp64": rel_err,
                       "ms": ms, "steps_per_s": args.k / (ms * 1e-3),
                       "per_kernel_ms": {k2: v[0] / args.repeats for k2, v in prof.items()},
                       "input_gb": D.input_bytes() / 1e9}))
