@@ -152,3 +152,17 @@ def test_config4_shape_n128():
     check(P, X, S)
     X2, _ = native.smooth(P, covariance=False, fp32_refine=True)
     assert oracle.rel_err_states(X2, X) < 1e-11
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_cta_path_every_length_1_to_17(fp32):
+    """The CTA kernels over every track length 1..17 (every parity of every
+    level, odd-length fix-ups, one-step base cases) in one batch, n = 10."""
+    P = pb.random_dynamics(list(range(1, 18)), 10, 5, seed=12, per_step=True, missing=0.15)
+    if fp32:
+        X, _ = native.smooth(P, covariance=False, fp32_refine=True)
+        st, Xo, _ = oracle.smooth(P, "oddeven", covariance=False)
+        assert st == 0 and oracle.rel_err_states(X, Xo) < 1e-9
+    else:
+        X, S = native.smooth(P)
+        check(P, X, S)
