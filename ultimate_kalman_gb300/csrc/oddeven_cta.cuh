@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(NT) weigh_cta(CArgs<T> a, RawA raw, int64_t ns
  * Scratch: the largest panel, 2n x (3n+1).
  * ------------------------------------------------------------------------ */
 template <typename T>
-__global__ void __launch_bounds__(NT) pair_cta(CArgs<T> a)
+__global__ void __launch_bounds__(NT, 4) pair_cta(CArgs<T> a)
 {
   __shared__ T red[33];
   const int n = a.n, mx = a.mx, tid = threadIdx.x;
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(NT) pair_cta(CArgs<T> a)
         A[e] = v;
       }
       __syncthreads();
-      ::cta::householder(A, ld, rows, n, ld, red);
+      ::cta::panel_qr(A, ld, rows, n, ld, red);
       for (int e = tid; e < n * n; e += NT) {
         const int r = e / n, c = e - r * n; /* R~ (r, c), Y~ (r, c) */
         Rr.R.at(c * n + r, se) = r <= c ? A[(int64_t)r * ld + c] : T(0);
@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(NT) pair_cta(CArgs<T> a)
         A[e] = v;
       }
       __syncthreads();
-      ::cta::householder(A, ld, rows, n, ld, red);
+      ::cta::panel_qr(A, ld, rows, n, ld, red);
       for (int e = tid; e < n * n; e += NT) {
         const int r = e / n, c = e - r * n;
         Rr.R.at(c * n + r, se) = r <= c ? A[(int64_t)r * ld + c] : T(0);
