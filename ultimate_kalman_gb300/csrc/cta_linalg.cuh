@@ -100,13 +100,19 @@ static __device__ void householder(T* A, int ld, int rows, int npiv, int cols, T
  * read from shared memory.  Same result as householder() up to rounding;
  * reflectors are stored below the diagonal in the same convention.          */
 constexpr int kWyNB = 16;
+constexpr int kWyRows = 8; /* trailing-column rows loaded together */
+
+/* shared-memory entries householder_wy works in: the panel (rows x kWyNB,
+ * zero-padded), the reflectors' Gram matrix, their tau factors, a norm */
+constexpr int kWyShared = kMaxPanelRows * kWyNB + kWyNB * kWyNB + kWyNB + 1;
 
 template <typename T>
-static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols, T* red)
+static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols, T* red, T* sh)
 {
-  __shared__ __align__(16) T Vs[kMaxPanelRows * kWyNB]; /* panel rows x kWyNB, zero-padded */
-  __shared__ T Gs[kWyNB * kWyNB];                       /* Gs[l * kWyNB + b] = v_l^T v_b, l < b */
-  __shared__ T taus[kWyNB];
+  T* Vs = sh;                              /* Vs[i * kWyNB + b] */
+  T* Gs = sh + kMaxPanelRows * kWyNB;      /* Gs[l * kWyNB + b] = v_l^T v_b, l < b */
+  T* taus = Gs + kWyNB * kWyNB;
+  T* nrm = taus + kWyNB;                   /* look-ahead norm of the next panel column */
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int kmax = rows < npiv ? rows : npiv;
   for (int k0 = 0; k0 < kmax; k0 += kWyNB) {
@@ -118,16 +124,23 @@ static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols
       Vs[e] = b < kb ? P[(int64_t)i * ld + b] : T(0);
     }
     __syncthreads();
+    bool ahead = false; /* the squared norm below the diagonal of column k was computed by the previous update */
     for (int k = 0; k < kb; ++k) {
-      T part = T(0);
-      for (int i = k + 1 + tid; i < prow; i += NT) {
-        const T x = Vs[i * kWyNB + k];
-        part = fma(x, x, part);
+      T tail;
+      if (ahead) {
+        tail = *nrm;
+      } else {
+        T part = T(0);
+        for (int i = k + 1 + tid; i < prow; i += NT) {
+          const T x = Vs[i * kWyNB + k];
+          part = fma(x, x, part);
+        }
+        tail = block_sum(part, red);
       }
-      const T tail = block_sum(part, red);
       const T alpha = Vs[k * kWyNB + k];
       if (tail == T(0)) { /* identity reflector: every thread agrees */
         if (tid == 0) taus[k] = T(0);
+        ahead = false;
         continue;
       }
       const T beta = -copysign(sqrt(fma(alpha, alpha, tail)), alpha);
@@ -141,7 +154,16 @@ static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols
         for (int i = k + 1 + lane; i < prow; i += 32) d = fma(Vs[i * kWyNB + k], Vs[i * kWyNB + j], d);
         for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xffffffffu, d, off);
         d = (d + Vs[k * kWyNB + j]) * t;
-        for (int i = k + 1 + lane; i < prow; i += 32) Vs[i * kWyNB + j] = fma(-d, Vs[i * kWyNB + k], Vs[i * kWyNB + j]);
+        T sq = T(0);
+        for (int i = k + 1 + lane; i < prow; i += 32) {
+          const T v = fma(-d, Vs[i * kWyNB + k], Vs[i * kWyNB + j]);
+          Vs[i * kWyNB + j] = v;
+          if (i > k + 1) sq = fma(v, v, sq);
+        }
+        if (j == k + 1) { /* the next column's norm, for the next reflector */
+          for (int off = 16; off > 0; off >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, off);
+          if (lane == 0) *nrm = sq;
+        }
         __syncwarp();
         if (lane == 0) Vs[k * kWyNB + j] -= d;
       }
@@ -149,6 +171,7 @@ static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols
         Vs[k * kWyNB + k] = beta;
         taus[k] = t;
       }
+      ahead = k + 1 < kb;
       __syncthreads();
     }
     /* R and the reflectors back to the panel; V in shared memory in unit form */
@@ -182,8 +205,20 @@ static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols
       T w[kWyNB];
 #pragma unroll
       for (int b = 0; b < kWyNB; ++b) w[b] = T(0);
+      /* rows in groups of kWyRows: their loads are in flight together */
+      int i = 0;
 #pragma unroll 1
-      for (int i = 0; i < prow; ++i) {
+      for (; i + kWyRows <= prow; i += kWyRows) {
+        T cv[kWyRows];
+#pragma unroll
+        for (int u = 0; u < kWyRows; ++u) cv[u] = C[(int64_t)(i + u) * ld + c];
+#pragma unroll
+        for (int u = 0; u < kWyRows; ++u)
+#pragma unroll
+          for (int b = 0; b < kWyNB; ++b) w[b] = fma(Vs[(i + u) * kWyNB + b], cv[u], w[b]);
+      }
+#pragma unroll 1
+      for (; i < prow; ++i) {
         const T ci = C[(int64_t)i * ld + c];
 #pragma unroll
         for (int b = 0; b < kWyNB; ++b) w[b] = fma(Vs[i * kWyNB + b], ci, w[b]);
@@ -199,8 +234,21 @@ static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols
         for (int l = 0; l < b; ++l) sm = fma(-Gs[g0 + l * kWyNB + b], w[l], sm);
         w[b] = taus[b < kb ? b : 0] * (b < kb ? sm : T(0)); /* w now holds u */
       }
-#pragma unroll 2
-      for (int i = 0; i < prow; ++i) {
+      i = 0;
+#pragma unroll 1
+      for (; i + kWyRows <= prow; i += kWyRows) {
+        T cv[kWyRows];
+#pragma unroll
+        for (int u = 0; u < kWyRows; ++u) cv[u] = C[(int64_t)(i + u) * ld + c];
+#pragma unroll
+        for (int u = 0; u < kWyRows; ++u) {
+#pragma unroll
+          for (int b = 0; b < kWyNB; ++b) cv[u] = fma(-Vs[(i + u) * kWyNB + b], w[b], cv[u]);
+          C[(int64_t)(i + u) * ld + c] = cv[u];
+        }
+      }
+#pragma unroll 1
+      for (; i < prow; ++i) {
         T ci = C[(int64_t)i * ld + c];
 #pragma unroll
         for (int b = 0; b < kWyNB; ++b) ci = fma(-Vs[i * kWyNB + b], w[b], ci);
@@ -211,16 +259,17 @@ static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols
   }
 }
 
-/* QR of a panel with whichever of the two forms suits its size: the blocked
- * form from 64 pivots (at n = 128 the odd-even pair kernel runs 2.3x faster
- * with it; at n = 48 the unblocked form is 13 % faster, its panels staying in
- * L1 next to the smaller shared-memory footprint) */
-template <typename T>
-static __device__ __forceinline__ void panel_qr(T* A, int ld, int rows, int npiv, int cols, T* red)
+/* QR of a panel with whichever of the two forms suits its size: kernels for
+ * states from 64 on instantiate the blocked form (at n = 128 the odd-even pair
+ * kernel runs 2.3x faster with it), the others keep the unblocked form and
+ * its small shared-memory footprint (at n = 48 the panels then stay in L1). */
+template <bool kBlocked, typename T>
+static __device__ __forceinline__ void panel_qr(T* A, int ld, int rows, int npiv, int cols, T* red, T* sh)
 {
-  if (npiv >= 4 * kWyNB && rows >= 4 * kWyNB && cols > npiv + kWyNB) householder_wy(A, ld, rows, npiv, cols, red);
+  if (kBlocked && npiv >= kWyNB && cols > npiv) householder_wy(A, ld, rows, npiv, cols, red, sh);
   else householder(A, ld, rows, npiv, cols, red);
 }
+constexpr int kBlockedMinN = 64;
 
 /* x <- R^{-1} x for every column c0 <= c < c1 of the row-major X (ldx), R the
  * upper triangle of the row-major Rm (ldr), n x n: one thread per column */
@@ -256,16 +305,187 @@ static __device__ void solve_upper_vec(const T* Rm, int ldr, int n, T* x)
 
 static __device__ __forceinline__ bool valid_cov_type(char t) { return t == 'W' || t == 'w' || t == 'C' || t == 'U' || t == 'F'; }
 
+/* Cholesky factor of an SPD matrix held column-major in L (rows x rows, ld
+ * rows; its lower triangle is read and overwritten, the strict upper triangle
+ * is ignored), blocked by kChNB columns: each column block is copied to
+ * shared memory and factored there, then the trailing lower triangle takes the
+ * block's rank-kChNB update, a warp per column with lanes along it (coalesced).
+ * A pivot that is not positive is replaced by 1 and reported: returns false
+ * in every thread.                                                           */
+constexpr int kChNB = 8;
+constexpr int kMaxCov = 128; /* largest covariance dimension of the CTA kernels */
+
+template <typename T>
+static __device__ bool cholesky_cm(T* L, int rows)
+{
+  __shared__ T Ps[kChNB][kMaxCov];
+  __shared__ int bad_c;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) bad_c = 0;
+  for (int j0 = 0; j0 < rows; j0 += kChNB) {
+    const int nb = rows - j0 < kChNB ? rows - j0 : kChNB;
+    for (int jj = warp; jj < kChNB; jj += NT / 32)
+      for (int i = j0 + lane; i < rows; i += 32) Ps[jj][i] = jj < nb ? L[(int64_t)(j0 + jj) * rows + i] : T(0);
+    __syncthreads();
+    for (int jj = 0; jj < nb; ++jj) {
+      const int j = j0 + jj;
+      if (tid == 0) {
+        const T d = Ps[jj][j];
+        if (!(d > T(0))) bad_c = 1;
+        Ps[jj][j] = d > T(0) ? sqrt(d) : T(1);
+      }
+      __syncthreads();
+      const T ljj = Ps[jj][j];
+      for (int i = j + 1 + tid; i < rows; i += NT) Ps[jj][i] /= ljj;
+      __syncthreads();
+      for (int kk = jj + 1 + warp; kk < nb; kk += NT / 32) {
+        const T mk = Ps[jj][j0 + kk];
+        for (int i = j0 + kk + lane; i < rows; i += 32) Ps[kk][i] = fma(-Ps[jj][i], mk, Ps[kk][i]);
+      }
+      __syncthreads();
+    }
+    for (int jj = warp; jj < nb; jj += NT / 32)
+      for (int i = j0 + jj + lane; i < rows; i += 32) L[(int64_t)(j0 + jj) * rows + i] = Ps[jj][i];
+    for (int l = j0 + nb + warp; l < rows; l += NT / 32) {
+      T pl[kChNB];
+#pragma unroll
+      for (int jj = 0; jj < kChNB; ++jj) pl[jj] = Ps[jj][l];
+      for (int i = l + lane; i < rows; i += 32) {
+        T v = L[(int64_t)l * rows + i];
+#pragma unroll
+        for (int jj = 0; jj < kChNB; ++jj) v = fma(-Ps[jj][i], pl[jj], v);
+        L[(int64_t)l * rows + i] = v;
+      }
+    }
+    __syncthreads();
+  }
+  const bool ok = bad_c == 0;
+  __syncthreads();
+  return ok;
+}
+
+/* B <- L^{-1} B for the row-major B (rows x cols, ldb) and the lower
+ * triangular, column-major L (ld rows): one thread per column, four rows at a
+ * time (each B entry loaded once per four rows, four independent chains).   */
+template <typename T>
+static __device__ void forward_subst_cm(const T* L, int rows, T* B, int ldb, int cols)
+{
+  for (int c = threadIdx.x; c < cols; c += NT)
+    for (int i0 = 0; i0 < rows; i0 += 4) {
+      const int nq = rows - i0 < 4 ? rows - i0 : 4;
+      T s[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) s[q] = q < nq ? B[(int64_t)(i0 + q) * ldb + c] : T(0);
+      if (nq == 4) {
+        for (int k = 0; k < i0; ++k) {
+          const T bk = B[(int64_t)k * ldb + c];
+          const T* Lk = L + (int64_t)k * rows + i0;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) s[q] = fma(-Lk[q], bk, s[q]);
+        }
+      } else {
+        for (int k = 0; k < i0; ++k) {
+          const T bk = B[(int64_t)k * ldb + c];
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (q < nq) s[q] = fma(-L[(int64_t)k * rows + i0 + q], bk, s[q]);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (q < nq) {
+#pragma unroll
+          for (int r = 0; r < q; ++r) s[q] = fma(-L[(int64_t)(i0 + r) * rows + i0 + q], s[r], s[q]);
+          s[q] /= L[(int64_t)(i0 + q) * rows + i0 + q];
+          B[(int64_t)(i0 + q) * ldb + c] = s[q];
+        }
+    }
+  __syncthreads();
+}
+
+/* w <- L^{-1} w (lower = true) or L^{-T} w for the column-major lower
+ * triangular L (ld rows) and the CTA-shared vector w; run by warp 0, columns of
+ * L read along their length, and followed by a CTA barrier.                 */
+template <typename T>
+static __device__ void tri_solve_vec_cm(const T* L, int rows, T* w, bool lower)
+{
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    if (lower)
+      for (int j = 0; j < rows; ++j) {
+        const T wj = w[j] / L[(int64_t)j * rows + j];
+        __syncwarp();
+        if (lane == 0) w[j] = wj;
+        for (int i = j + 1 + lane; i < rows; i += 32) w[i] = fma(-L[(int64_t)j * rows + i], wj, w[i]);
+        __syncwarp();
+      }
+    else
+      for (int j = rows - 1; j >= 0; --j) {
+        T d = T(0);
+        for (int i = j + 1 + lane; i < rows; i += 32) d = fma(L[(int64_t)j * rows + i], w[i], d);
+        for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xffffffffu, d, off);
+        const T wj = (w[j] - d) / L[(int64_t)j * rows + j];
+        __syncwarp();
+        if (lane == 0) w[j] = wj;
+        __syncwarp();
+      }
+  }
+  __syncthreads();
+}
+
+/* Copies between a column-major block (ld lds) and a row-major block (ld ldd)
+ * through a 32 x 33 shared tile, so that both sides are read and written
+ * along rows of 32 consecutive entries.  f converts each element.           */
+template <typename T>
+struct Tile {
+  T t[32][33];
+};
+template <typename D, typename S, typename F>
+static __device__ void cm_to_rm(const S* src, int64_t lds, int rows, int cols, D* dst, int64_t ldd, F f, Tile<D>& tl)
+{
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int r0 = 0; r0 < rows; r0 += 32)
+    for (int c0 = 0; c0 < cols; c0 += 32) {
+      for (int cc = warp; cc < 32; cc += NT / 32)
+        if (c0 + cc < cols && r0 + lane < rows) tl.t[cc][lane] = f(src[(int64_t)(c0 + cc) * lds + r0 + lane]);
+      __syncthreads();
+      for (int rr = warp; rr < 32; rr += NT / 32)
+        if (r0 + rr < rows && c0 + lane < cols) dst[(int64_t)(r0 + rr) * ldd + c0 + lane] = tl.t[lane][rr];
+      __syncthreads();
+    }
+}
+struct Ident {
+  template <typename V>
+  __device__ __forceinline__ V operator()(V v) const { return v; }
+};
+/* kUpper: entries below the diagonal are written as zeros */
+template <bool kUpper = false, typename D, typename S>
+static __device__ void rm_to_cm(const S* src, int64_t lds, int rows, int cols, D* dst, int64_t ldd, Tile<S>& tl)
+{
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int r0 = 0; r0 < rows; r0 += 32)
+    for (int c0 = 0; c0 < cols; c0 += 32) {
+      for (int rr = warp; rr < 32; rr += NT / 32)
+        if (r0 + rr < rows && c0 + lane < cols) tl.t[rr][lane] = src[(int64_t)(r0 + rr) * lds + c0 + lane];
+      __syncthreads();
+      for (int cc = warp; cc < 32; cc += NT / 32)
+        if (c0 + cc < cols && r0 + lane < rows)
+          dst[(int64_t)(c0 + cc) * ldd + r0 + lane] = kUpper && r0 + lane > c0 + cc ? D(0) : tl.t[lane][cc];
+      __syncthreads();
+    }
+}
+
 /* Weighs the row-major panel B (rows x cols, ldb) by the covariance factor
  * (cov column-major rows x rows, ld ldc, type): 'W' B <- W B, 'w' B <- diag B,
- * 'C' B <- chol(cov)^{-1} B, 'U'/'F' B <- tril(cov)^{-1} B.  L (rows x rows
- * row-major, ld rows) is scratch.  Returns false (in every thread) for a
- * factor that is not positive definite or has a zero pivot. */
+ * 'C' B <- chol(cov)^{-1} B, 'U'/'F' B <- tril(cov)^{-1} B (the lower
+ * triangle of cov in both).  L (rows x rows) is scratch, used column-major.
+ * Returns false (in every thread) for a factor that is not positive definite
+ * or has a zero pivot. */
 template <typename T>
 static __device__ bool weigh_panel(char type, const double* cov, int ldc, int rows, T* B, int ldb, int cols, T* L,
                                   T* red, T* tmp)
 {
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (type == 'w') {
     for (int e = tid; e < rows * cols; e += NT) {
       const int i = e / cols, c = e - i * cols;
@@ -277,9 +497,14 @@ static __device__ bool weigh_panel(char type, const double* cov, int ldc, int ro
   if (type == 'W') { /* B <- W B, one thread per column, W read from the caller's array */
     for (int c = tid; c < cols; c += NT) {
       for (int i = 0; i < rows; ++i) {
-        T s = T(0);
-        for (int j = 0; j < rows; ++j) s = fma(T(cov[(int64_t)j * ldc + i]), B[(int64_t)j * ldb + c], s);
-        tmp[(int64_t)i * NT + tid] = s;
+        T s0 = T(0), s1 = T(0);
+        int j = 0;
+        for (; j + 1 < rows; j += 2) {
+          s0 = fma(T(cov[(int64_t)j * ldc + i]), B[(int64_t)j * ldb + c], s0);
+          s1 = fma(T(cov[(int64_t)(j + 1) * ldc + i]), B[(int64_t)(j + 1) * ldb + c], s1);
+        }
+        if (j < rows) s0 = fma(T(cov[(int64_t)j * ldc + i]), B[(int64_t)j * ldb + c], s0);
+        tmp[(int64_t)i * NT + tid] = s0 + s1;
       }
       for (int i = 0; i < rows; ++i) B[(int64_t)i * ldb + c] = tmp[(int64_t)i * NT + tid];
     }
@@ -287,47 +512,24 @@ static __device__ bool weigh_panel(char type, const double* cov, int ldc, int ro
     return true;
   }
   if (type != 'C' && type != 'U' && type != 'F') return true;
-  for (int e = tid; e < rows * rows; e += NT) {
-    const int i = e / rows, j = e - i * rows;
-    L[e] = i >= j ? T(cov[(int64_t)j * ldc + i]) : T(0);
-  }
+  for (int j = warp; j < rows; j += NT / 32)
+    for (int i = lane; i < rows; i += 32) L[(int64_t)j * rows + i] = i >= j ? T(cov[(int64_t)j * ldc + i]) : T(0);
   __syncthreads();
-  __shared__ int bad_s;
-  if (tid == 0) bad_s = 0;
-  __syncthreads();
-  if (type == 'C') { /* right-looking Cholesky, in place in L */
-    for (int j = 0; j < rows; ++j) {
-      if (tid == 0) {
-        const T d = L[(int64_t)j * rows + j];
-        if (!(d > T(0))) bad_s = 1;
-        L[(int64_t)j * rows + j] = d > T(0) ? sqrt(d) : T(1);
-      }
-      __syncthreads();
-      const T ljj = L[(int64_t)j * rows + j];
-      for (int i = j + 1 + tid; i < rows; i += NT) L[(int64_t)i * rows + j] /= ljj;
-      __syncthreads();
-      for (int i = j + 1 + tid; i < rows; i += NT) {
-        const T lij = L[(int64_t)i * rows + j];
-        for (int l = j + 1; l <= i; ++l) L[(int64_t)i * rows + l] = fma(-lij, L[(int64_t)l * rows + j], L[(int64_t)i * rows + l]);
-      }
-      __syncthreads();
-    }
+  bool ok = true;
+  if (type == 'C') {
+    ok = cholesky_cm(L, rows);
   } else {
-    if (tid == 0)
+    __shared__ int bad_s;
+    if (tid == 0) {
+      bad_s = 0;
       for (int j = 0; j < rows; ++j)
         if (L[(int64_t)j * rows + j] == T(0)) bad_s = 1;
+    }
+    __syncthreads();
+    ok = bad_s == 0;
     __syncthreads();
   }
-  /* forward substitution, one thread per column */
-  for (int c = tid; c < cols; c += NT)
-    for (int i = 0; i < rows; ++i) {
-      T s = B[(int64_t)i * ldb + c];
-      for (int k = 0; k < i; ++k) s = fma(-L[(int64_t)i * rows + k], B[(int64_t)k * ldb + c], s);
-      B[(int64_t)i * ldb + c] = s / L[(int64_t)i * rows + i];
-    }
-  __syncthreads();
-  const bool ok = bad_s == 0;
-  __syncthreads();
+  forward_subst_cm(L, rows, B, ldb, cols);
   return ok;
 }
 

@@ -2973,7 +2973,12 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
     common(a, l);
     a.ce = eq_level(l);
     if (l + 1 < nlev) a.ne = eq_level(l + 1);
-    if (lp[l].npairs > 0) UKG_LAUNCH(kPair, st, (ctak::pair_cta<T><<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
+    if (lp[l].npairs > 0) {
+      if (n >= cta::kBlockedMinN)
+        UKG_LAUNCH(kPair, st, (ctak::pair_cta<T, true><<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
+      else
+        UKG_LAUNCH(kPair, st, (ctak::pair_cta<T, false><<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
+    }
     if (lp[l].ntail > 0) UKG_LAUNCH(UKG_K_TAIL, st, (ctak::tail_cta<T><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
   }
   for (int l = nlev - 2; l >= 0; --l) {

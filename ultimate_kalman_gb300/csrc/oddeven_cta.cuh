@@ -65,9 +65,19 @@ struct RawA {
  * Scratch: n^2 (L) + n (2n+1) (panel) + rows x NT (the 'W' product).
  * ------------------------------------------------------------------------ */
 template <typename T>
+struct Narrow {
+  __device__ __forceinline__ T operator()(double v) const { return ukg_df::narrow<T>(v); }
+};
+template <typename T>
+struct NegNarrow {
+  __device__ __forceinline__ T operator()(double v) const { return -ukg_df::narrow<T>(v); }
+};
+
+template <typename T>
 __global__ void __launch_bounds__(NT) weigh_cta(CArgs<T> a, RawA raw, int64_t nsteps)
 {
   __shared__ T red[33];
+  __shared__ Tile<T> tl;
   const int n = a.n, mx = a.mx, mm = raw.mmax, tid = threadIdx.x;
   const int rmax = n > mm ? n : mm;
   T* L = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
@@ -80,24 +90,16 @@ __global__ void __launch_bounds__(NT) weigh_cta(CArgs<T> a, RawA raw, int64_t ns
     bool bad = false;
     if (i > 0) {
       const int ld = 2 * n + 1;
-      for (int e = tid; e < n * ld; e += NT) {
-        const int r = e / ld, c = e - r * ld;
-        T v;
-        if (c < n) v = ukg_df::narrow<T>(raw.H[g * nn + (int64_t)c * n + r]);
-        else if (c < 2 * n) v = -ukg_df::narrow<T>(raw.F[g * nn + (int64_t)(c - n) * n + r]);
-        else v = ukg_df::narrow<T>(raw.c[g * n + r]);
-        B[e] = v;
-      }
+      cm_to_rm(raw.H + g * nn, n, n, n, B, ld, Narrow<T>(), tl);
+      cm_to_rm(raw.F + g * nn, n, n, n, B + n, ld, NegNarrow<T>(), tl);
+      for (int r = tid; r < n; r += NT) B[(int64_t)r * ld + 2 * n] = ukg_df::narrow<T>(raw.c[g * n + r]);
       __syncthreads();
       const char kt = raw.K_type[g];
       if (tid == 0 && !valid_cov_type(kt)) atomicOr(a.flag, 4);
       bad |= !weigh_panel(kt, raw.K + g * nn, n, n, B, ld, ld, L, red, tmp);
-      for (int e = tid; e < n * ld; e += NT) {
-        const int r = e / ld, c = e - r * ld;
-        if (c < n) a.ce.H.at(c * n + r, q) = B[e];
-        else if (c < 2 * n) a.ce.F.at((c - n) * n + r, q) = B[e];
-        else a.ce.c.at(r, q) = B[e];
-      }
+      rm_to_cm(B, ld, n, n, &a.ce.H.at(0, q), n, tl);
+      rm_to_cm(B + n, ld, n, n, &a.ce.F.at(0, q), n, tl);
+      for (int r = tid; r < n; r += NT) a.ce.c.at(r, q) = B[(int64_t)r * ld + 2 * n];
       __syncthreads();
     }
     int m = raw.obs_rows[g];
@@ -108,19 +110,14 @@ __global__ void __launch_bounds__(NT) weigh_cta(CArgs<T> a, RawA raw, int64_t ns
     if (tid == 0) a.ce.m[q] = m;
     if (m > 0) {
       const int ld = n + 1;
-      for (int e = tid; e < m * ld; e += NT) {
-        const int r = e / ld, c = e - r * ld;
-        B[e] = ukg_df::narrow<T>(c < n ? raw.G[g * (int64_t)mm * n + (int64_t)c * mm + r] : raw.o[g * mm + r]);
-      }
+      cm_to_rm(raw.G + g * (int64_t)mm * n, mm, m, n, B, ld, Narrow<T>(), tl);
+      for (int r = tid; r < m; r += NT) B[(int64_t)r * ld + n] = ukg_df::narrow<T>(raw.o[g * mm + r]);
       __syncthreads();
       const char ct = raw.C_type[g];
       if (tid == 0 && !valid_cov_type(ct)) atomicOr(a.flag, 4);
       bad |= !weigh_panel(ct, raw.C + g * (int64_t)mm * mm, mm, m, B, ld, ld, L, red, tmp);
-      for (int e = tid; e < m * ld; e += NT) {
-        const int r = e / ld, c = e - r * ld;
-        if (c < n) a.ce.G.at(c * mx + r, q) = B[e];
-        else a.ce.o.at(r, q) = B[e];
-      }
+      rm_to_cm(B, ld, m, n, &a.ce.G.at(0, q), mx, tl);
+      for (int r = tid; r < m; r += NT) a.ce.o.at(r, q) = B[(int64_t)r * ld + n];
       __syncthreads();
     }
     if (bad && tid == 0) atomicOr(a.flag, 1);
@@ -131,10 +128,11 @@ __global__ void __launch_bounds__(NT) weigh_cta(CArgs<T> a, RawA raw, int64_t ns
  * forward elimination of one pair per CTA: stages A, C, B
  * Scratch: the largest panel, 2n x (3n+1).
  * ------------------------------------------------------------------------ */
-template <typename T>
+template <typename T, bool kBlocked>
 __global__ void __launch_bounds__(NT, 4) pair_cta(CArgs<T> a)
 {
   __shared__ T red[33];
+  __shared__ __align__(16) T sh[kBlocked ? kWyShared : 1]; /* the blocked QR's panel */
   const int n = a.n, mx = a.mx, tid = threadIdx.x;
   T* A = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
   const EqA<T>& C = a.ce;
@@ -161,7 +159,7 @@ __global__ void __launch_bounds__(NT, 4) pair_cta(CArgs<T> a)
         A[e] = v;
       }
       __syncthreads();
-      ::cta::panel_qr(A, ld, rows, n, ld, red);
+      ::cta::panel_qr<kBlocked>(A, ld, rows, n, ld, red, sh);
       for (int e = tid; e < n * n; e += NT) {
         const int r = e / n, c = e - r * n; /* R~ (r, c), Y~ (r, c) */
         Rr.R.at(c * n + r, se) = r <= c ? A[(int64_t)r * ld + c] : T(0);
@@ -217,7 +215,7 @@ __global__ void __launch_bounds__(NT, 4) pair_cta(CArgs<T> a)
         A[e] = v;
       }
       __syncthreads();
-      ::cta::panel_qr(A, ld, rows, n, ld, red);
+      ::cta::panel_qr<kBlocked>(A, ld, rows, n, ld, red, sh);
       for (int e = tid; e < n * n; e += NT) {
         const int r = e / n, c = e - r * n;
         Rr.R.at(c * n + r, se) = r <= c ? A[(int64_t)r * ld + c] : T(0);
@@ -486,7 +484,7 @@ __global__ void __launch_bounds__(NT) solve_cta(CArgs<T> a, int want_cov)
  * 'W' W^T W, 'w' diag(cov)^2.  w and tmp are vectors shared by the CTA. */
 __device__ void apply_precision_cta(char type, const double* cov, int ldc, int rows, double* L, double* w, double* tmp)
 {
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (type == 'w') {
     for (int i = tid; i < rows; i += NT) w[i] *= cov[i] * cov[i];
     __syncthreads();
@@ -499,50 +497,22 @@ __device__ void apply_precision_cta(char type, const double* cov, int ldc, int r
       tmp[i] = sm;
     }
     __syncthreads();
-    for (int j = tid; j < rows; j += NT) {
+    for (int j = warp; j < rows; j += NT / 32) { /* w_j = sum_i W(i, j) tmp_i: column j along the lanes */
       double sm = 0.0;
-      for (int i = 0; i < rows; ++i) sm = fma(cov[(int64_t)j * ldc + i], tmp[i], sm);
-      w[j] = sm;
+      for (int i = lane; i < rows; i += 32) sm = fma(cov[(int64_t)j * ldc + i], tmp[i], sm);
+      for (int off = 16; off > 0; off >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, off);
+      if (lane == 0) w[j] = sm;
     }
     __syncthreads();
     return;
   }
   if (type != 'C' && type != 'U' && type != 'F') return;
-  for (int e = tid; e < rows * rows; e += NT) {
-    const int i = e / rows, j = e - i * rows;
-    L[e] = i >= j ? cov[(int64_t)j * ldc + i] : 0.0;
-  }
+  for (int j = warp; j < rows; j += NT / 32)
+    for (int i = lane; i < rows; i += 32) L[(int64_t)j * rows + i] = i >= j ? cov[(int64_t)j * ldc + i] : 0.0;
   __syncthreads();
-  if (type == 'C')
-    for (int j = 0; j < rows; ++j) {
-      if (tid == 0) {
-        const double d = L[(int64_t)j * rows + j];
-        L[(int64_t)j * rows + j] = d > 0.0 ? sqrt(d) : 1.0; /* the weighing reports a bad factor */
-      }
-      __syncthreads();
-      const double ljj = L[(int64_t)j * rows + j];
-      for (int i = j + 1 + tid; i < rows; i += NT) L[(int64_t)i * rows + j] /= ljj;
-      __syncthreads();
-      for (int i = j + 1 + tid; i < rows; i += NT) {
-        const double lij = L[(int64_t)i * rows + j];
-        for (int l = j + 1; l <= i; ++l) L[(int64_t)i * rows + l] = fma(-lij, L[(int64_t)l * rows + j], L[(int64_t)i * rows + l]);
-      }
-      __syncthreads();
-    }
-  for (int j = 0; j < rows; ++j) { /* L^{-1} w */
-    if (tid == 0) w[j] /= L[(int64_t)j * rows + j];
-    __syncthreads();
-    const double wj = w[j];
-    for (int i = j + 1 + tid; i < rows; i += NT) w[i] = fma(-L[(int64_t)i * rows + j], wj, w[i]);
-    __syncthreads();
-  }
-  for (int j = rows - 1; j >= 0; --j) { /* L^{-T} w */
-    if (tid == 0) w[j] /= L[(int64_t)j * rows + j];
-    __syncthreads();
-    const double wj = w[j];
-    for (int i = tid; i < j; i += NT) w[i] = fma(-L[(int64_t)j * rows + i], wj, w[i]);
-    __syncthreads();
-  }
+  if (type == 'C') cholesky_cm(L, rows); /* the weighing reports a bad factor */
+  tri_solve_vec_cm(L, rows, w, true);
+  tri_solve_vec_cm(L, rows, w, false);
 }
 
 __global__ void __launch_bounds__(NT) residual_cta(CArgs<float> a, RawA raw, Soa<double> wE, Soa<double> zp,
@@ -572,10 +542,11 @@ __global__ void __launch_bounds__(NT) residual_cta(CArgs<float> a, RawA raw, Soa
       __syncthreads();
       apply_precision_cta(raw.K_type[g], raw.K + g * nn, n, n, L, w, tmp);
       for (int r = tid; r < n; r += NT) wE.at(r, q) = w[r];
-      for (int c = tid; c < n; c += NT) {
+      for (int c = tid >> 5; c < n; c += NT / 32) { /* z = H^T w, column c of H along the lanes */
         double sm = 0.0;
-        for (int r = 0; r < n; ++r) sm = fma(H[(int64_t)c * n + r], w[r], sm);
-        z[c] = sm;
+        for (int r = tid & 31; r < n; r += 32) sm = fma(H[(int64_t)c * n + r], w[r], sm);
+        for (int off = 16; off > 0; off >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, off);
+        if ((tid & 31) == 0) z[c] = sm;
       }
       __syncthreads();
     }
@@ -589,10 +560,11 @@ __global__ void __launch_bounds__(NT) residual_cta(CArgs<float> a, RawA raw, Soa
       }
       __syncthreads();
       apply_precision_cta(raw.C_type[g], raw.C + g * (int64_t)mm * mm, mm, m, L, w, tmp);
-      for (int c = tid; c < n; c += NT) {
-        double sm = z[c];
-        for (int r = 0; r < m; ++r) sm = fma(G[(int64_t)c * mm + r], w[r], sm);
-        z[c] = sm;
+      for (int c = tid >> 5; c < n; c += NT / 32) {
+        double sm = 0.0;
+        for (int r = tid & 31; r < m; r += 32) sm = fma(G[(int64_t)c * mm + r], w[r], sm);
+        for (int off = 16; off > 0; off >>= 1) sm += __shfl_xor_sync(0xffffffffu, sm, off);
+        if ((tid & 31) == 0) z[c] += sm;
       }
       __syncthreads();
     }
