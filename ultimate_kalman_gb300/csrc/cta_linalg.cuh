@@ -103,17 +103,22 @@ constexpr int kWyNB = 16;
 constexpr int kWyRows = 8; /* trailing-column rows loaded together */
 
 /* shared-memory entries householder_wy works in: the panel (rows x kWyNB,
- * zero-padded), the reflectors' Gram matrix, their tau factors, a norm */
-constexpr int kWyShared = kMaxPanelRows * kWyNB + kWyNB * kWyNB + kWyNB + 1;
+ * zero-padded), the reflectors' Gram matrix, their tau factors and column
+ * scales, partial dot products (4 warps x kWyNB), look-ahead norms (4) */
+constexpr int kWyShared = kMaxPanelRows * kWyNB + kWyNB * kWyNB + 2 * kWyNB + 4 * kWyNB + 4;
 
 template <typename T>
 static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols, T* red, T* sh)
 {
+  static_assert(NT == 8 * kWyNB, "the panel factorization maps the CTA to kWyNB columns x 8 row groups");
   T* Vs = sh;                              /* Vs[i * kWyNB + b] */
   T* Gs = sh + kMaxPanelRows * kWyNB;      /* Gs[l * kWyNB + b] = v_l^T v_b, l < b */
   T* taus = Gs + kWyNB * kWyNB;
-  T* nrm = taus + kWyNB;                   /* look-ahead norm of the next panel column */
+  T* scl = taus + kWyNB;                   /* reflector b's entries below the diagonal, unscaled until write-back */
+  T* dpart = scl + kWyNB;                  /* [warp][column] */
+  T* nrm4 = dpart + 4 * kWyNB;             /* [warp]: look-ahead norm of the next column */
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int jc = tid & (kWyNB - 1), rg = tid >> 4; /* panel factorization: column, row group */
   const int kmax = rows < npiv ? rows : npiv;
   for (int k0 = 0; k0 < kmax; k0 += kWyNB) {
     const int kb = kmax - k0 < kWyNB ? kmax - k0 : kWyNB;
@@ -124,11 +129,15 @@ static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols
       Vs[e] = b < kb ? P[(int64_t)i * ld + b] : T(0);
     }
     __syncthreads();
-    bool ahead = false; /* the squared norm below the diagonal of column k was computed by the previous update */
+    /* panel factorization, thread (jc, rg) on column jc, rows rg, rg + 8, ...:
+       reflector k is x (column k below the diagonal, left unscaled) times
+       scale; for each later column j, d_j = tau (a_kj + scale x^T a_j) and
+       a_j <- a_j - d_j scale x; two barriers per reflector */
+    bool ahead = false;
     for (int k = 0; k < kb; ++k) {
       T tail;
       if (ahead) {
-        tail = *nrm;
+        tail = (nrm4[0] + nrm4[1]) + (nrm4[2] + nrm4[3]);
       } else {
         T part = T(0);
         for (int i = k + 1 + tid; i < prow; i += NT) {
@@ -139,7 +148,10 @@ static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols
       }
       const T alpha = Vs[k * kWyNB + k];
       if (tail == T(0)) { /* identity reflector: every thread agrees */
-        if (tid == 0) taus[k] = T(0);
+        if (tid == 0) {
+          taus[k] = T(0);
+          scl[k] = T(1);
+        }
         ahead = false;
         continue;
       }
@@ -147,40 +159,43 @@ static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols
       const T amb = alpha - beta;
       const T inv = T(1) / (beta * amb);
       const T t = -(amb * amb) * inv, scale = beta * inv;
-      for (int i = k + 1 + tid; i < prow; i += NT) Vs[i * kWyNB + k] *= scale;
+      const bool act = jc > k && jc < kb;
+      const T akj = act ? Vs[k * kWyNB + jc] : T(0);
+      T part = T(0);
+      if (act)
+        for (int i = k + 1 + rg; i < prow; i += 8) part = fma(Vs[i * kWyNB + k], Vs[i * kWyNB + jc], part);
+      part += __shfl_xor_sync(0xffffffffu, part, 16);
+      if (lane < 16) dpart[warp * kWyNB + jc] = part;
       __syncthreads();
-      for (int j = k + 1 + warp; j < kb; j += NT / 32) {
-        T d = T(0);
-        for (int i = k + 1 + lane; i < prow; i += 32) d = fma(Vs[i * kWyNB + k], Vs[i * kWyNB + j], d);
-        for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xffffffffu, d, off);
-        d = (d + Vs[k * kWyNB + j]) * t;
-        T sq = T(0);
-        for (int i = k + 1 + lane; i < prow; i += 32) {
-          const T v = fma(-d, Vs[i * kWyNB + k], Vs[i * kWyNB + j]);
-          Vs[i * kWyNB + j] = v;
+      const T d = act ? (akj + scale * ((dpart[jc] + dpart[kWyNB + jc]) + (dpart[2 * kWyNB + jc] + dpart[3 * kWyNB + jc]))) * t
+                      : T(0);
+      const T ds = d * scale;
+      T sq = T(0);
+      if (act)
+        for (int i = k + 1 + rg; i < prow; i += 8) {
+          const T v = fma(-ds, Vs[i * kWyNB + k], Vs[i * kWyNB + jc]);
+          Vs[i * kWyNB + jc] = v;
           if (i > k + 1) sq = fma(v, v, sq);
         }
-        if (j == k + 1) { /* the next column's norm, for the next reflector */
-          for (int off = 16; off > 0; off >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, off);
-          if (lane == 0) *nrm = sq;
-        }
-        __syncwarp();
-        if (lane == 0) Vs[k * kWyNB + j] -= d;
-      }
+      sq += __shfl_xor_sync(0xffffffffu, sq, 16);
+      if (k + 1 < kb && lane == k + 1) nrm4[warp] = sq; /* column k + 1's lanes are k + 1 and k + 17 */
+      if (act && rg == 0) Vs[k * kWyNB + jc] = akj - d;
       if (tid == 0) {
         Vs[k * kWyNB + k] = beta;
         taus[k] = t;
+        scl[k] = scale;
       }
       ahead = k + 1 < kb;
       __syncthreads();
     }
-    /* R and the reflectors back to the panel; V in shared memory in unit form */
+    /* R and the scaled reflectors back to the panel; V in shared memory in unit form */
     for (int e = tid; e < prow * kWyNB; e += NT) {
       const int i = e / kWyNB, b = e - i * kWyNB;
       if (b < kb) {
-        const T v = Vs[e];
+        T v = Vs[e];
+        if (i > b) v *= scl[b];
         P[(int64_t)i * ld + b] = v;
-        if (i <= b) Vs[e] = i == b ? T(1) : T(0);
+        Vs[e] = i > b ? v : i == b ? T(1) : T(0);
       }
     }
     __syncthreads();

@@ -2860,6 +2860,8 @@ extern "C" void ukg_release_oddeven_workspace(void)
  * ------------------------------------------------------------------------ */
 constexpr int kCtaMinN = 9; /* per-thread kernels below, CTA kernels from here on */
 constexpr int kCtaMaxN = 128;
+static_assert(kCtaMaxN <= 32 * ctak::kRtQ && kCtaMaxN <= cta::kMaxCov && 2 * kCtaMaxN <= cta::kMaxPanelRows,
+              "CTA kernels: per-lane state registers, covariance and panel buffers");
 
 int64_t cta_scratch_per_cta(int n, int mmax)
 {
@@ -2979,7 +2981,12 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
       else
         UKG_LAUNCH(kPair, st, (ctak::pair_cta<T, false><<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
     }
-    if (lp[l].ntail > 0) UKG_LAUNCH(UKG_K_TAIL, st, (ctak::tail_cta<T><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
+    if (lp[l].ntail > 0) {
+      if (n >= cta::kBlockedMinN)
+        UKG_LAUNCH(UKG_K_TAIL, st, (ctak::tail_cta<T, true><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
+      else
+        UKG_LAUNCH(UKG_K_TAIL, st, (ctak::tail_cta<T, false><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
+    }
   }
   for (int l = nlev - 2; l >= 0; --l) {
     ctak::CArgs<T> a;
@@ -3031,11 +3038,11 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
         Soa<float> yc{(float*)(B + P.o_y[l]), std::max<int64_t>(lp[l].E, 1)};
         if (lp[l].nsolve > 0)
           UKG_LAUNCH(UKG_K_RT, st,
-                     (ctak::rt_even_aos<<<(unsigned)((lp[l].nsolve + 127) / 128), 128, 0, st>>>(ca, zc, yc)));
+                     (ctak::rt_even_aos<<<(unsigned)((lp[l].nsolve * 32 + 127) / 128), 128, 0, st>>>(ca, zc, yc)));
         if (lp[l].npairs > 0 && l + 1 < nlev) {
           Soa<float> zn{(float*)(B + P.o_z[l + 1]), std::max<int64_t>(lp[l + 1].S, 1)};
           UKG_LAUNCH(UKG_K_RT, st,
-                     (ctak::rt_odd_aos<<<(unsigned)((lp[l].npairs + 127) / 128), 128, 0, st>>>(ca, zc, yc, zn)));
+                     (ctak::rt_odd_aos<<<(unsigned)((lp[l].npairs * 32 + 127) / 128), 128, 0, st>>>(ca, zc, yc, zn)));
         }
         if (lp[l].ntail > 0) {
           Soa<float> tmp{(float*)(B + P.o_tmp), std::max(T_, 1)};

@@ -237,10 +237,11 @@ __global__ void __launch_bounds__(NT, 4) pair_cta(CArgs<T> a)
  * odd-length tracks: the single last step and its fix-up, or the base case.
  * Scratch: the (n+m) x (2n+1) panel, an n x n inverse, an n-vector.
  * ------------------------------------------------------------------------ */
-template <typename T>
+template <typename T, bool kBlocked>
 __global__ void __launch_bounds__(NT) tail_cta(CArgs<T> a)
 {
   __shared__ T red[33];
+  __shared__ __align__(16) T sh[kBlocked ? kWyShared : 1]; /* the blocked QR's panel */
   const int n = a.n, mx = a.mx, tid = threadIdx.x;
   T* A = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
   const EqA<T>& C = a.ce;
@@ -326,7 +327,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs<T> a)
       WT[e] = v;
     }
     __syncthreads();
-    ::cta::householder(WT, ldT, rowsT, n, ldT, red);
+    ::cta::panel_qr<kBlocked>(WT, ldT, rowsT, n, ldT, red, sh);
     for (int e = tid; e < n * n; e += NT) {
       const int r = e / n, c = e - r * n;
       Rr.R.at(c * n + r, es) = r <= c ? WT[(int64_t)r * ldT + c] : T(0);
@@ -573,40 +574,79 @@ __global__ void __launch_bounds__(NT) residual_cta(CArgs<float> a, RawA raw, Soa
   }
 }
 
-/* refinement transpose solves over slot-major FP32 records, one thread per
- * item (as rt_even_kernel / rt_odd_kernel):
+/* refinement transpose solves over slot-major FP32 records, one warp per
+ * item (as rt_even_kernel / rt_odd_kernel), state entries k = lane + 32 q
+ * (q < 4: n <= 128) held in registers, record columns read along the lanes:
  *   even steps  y_j = R_j^{-T} z_j
  *   odd steps   z' = z_{2p+1} - Y_{2p}^T y_{2p} - Ft_{2p+2}^T y_{2p+2}      */
+constexpr int kRtQ = 4;
+
+static __device__ __forceinline__ float warp_sum(float v)
+{
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
 __global__ void rt_even_aos(CArgs<float> a, Soa<float> zc, Soa<float> yc)
 {
-  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (item >= a.ct.nsolve) return;
-  const int n = a.n;
+  const int64_t item = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (item >= a.ct.nsolve) return; /* uniform over the warp */
+  const int lane = threadIdx.x & 31, n = a.n;
   const int t = find_track(a.ct.solve, a.ntracks, item);
   const int64_t sz = a.ct.slot[t] + 2 * (item - a.ct.solve[t]);
+  const float* Rp = &a.cr.R.at(0, item); /* column i of R (entries k < i) at Rp[i * n + k] */
+  float yr[kRtQ];
+#pragma unroll
+  for (int q = 0; q < kRtQ; ++q) yr[q] = 0.f;
   for (int i = 0; i < n; ++i) {
-    float s = zc.at(i, sz);
-    for (int k = 0; k < i; ++k) s = fmaf(-a.cr.R.at(i * n + k, item), yc.at(k, item), s);
-    yc.at(i, item) = s / a.cr.R.at(i * n + i, item);
+    float d = 0.f;
+#pragma unroll
+    for (int q = 0; q < kRtQ; ++q) {
+      const int k = lane + 32 * q;
+      if (k < i) d = fmaf(Rp[(int64_t)i * n + k], yr[q], d);
+    }
+    d = warp_sum(d);
+    const float yi = (zc.at(i, sz) - d) / Rp[(int64_t)i * n + i];
+#pragma unroll
+    for (int q = 0; q < kRtQ; ++q)
+      if (i == lane + 32 * q) yr[q] = yi;
   }
+#pragma unroll
+  for (int q = 0; q < kRtQ; ++q)
+    if (lane + 32 * q < n) yc.at(lane + 32 * q, item) = yr[q];
 }
 
 __global__ void rt_odd_aos(CArgs<float> a, Soa<float> zc, Soa<float> yc, Soa<float> zn)
 {
-  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (item >= a.ct.npairs) return;
-  const int n = a.n;
+  const int64_t item = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (item >= a.ct.npairs) return; /* uniform over the warp */
+  const int lane = threadIdx.x & 31, n = a.n;
   const int t = find_track(a.ct.pair, a.ntracks, item);
   const int64_t p = item - a.ct.pair[t], L = a.ct.L[t];
   const int64_t so = a.ct.slot[t] + 2 * p + 1, sn = a.nt.slot[t] + p;
   const int64_t e0 = a.ct.solve[t] + p, e1 = e0 + 1;
   const bool right = 2 * p + 2 <= L - 1;
+  const float* Yp = &a.cr.Y.at(0, e0);
+  const float* Fp = &a.cr.Ft.at(0, right ? e1 : e0);
+  float y0[kRtQ], y1[kRtQ];
+#pragma unroll
+  for (int q = 0; q < kRtQ; ++q) {
+    const int r = lane + 32 * q;
+    y0[q] = r < n ? yc.at(r, e0) : 0.f;
+    y1[q] = r < n && right ? yc.at(r, e1) : 0.f;
+  }
   for (int c = 0; c < n; ++c) {
-    float s = zc.at(c, so);
-    for (int r = 0; r < n; ++r) s = fmaf(-a.cr.Y.at(c * n + r, e0), yc.at(r, e0), s);
-    if (right)
-      for (int r = 0; r < n; ++r) s = fmaf(-a.cr.Ft.at(c * n + r, e1), yc.at(r, e1), s);
-    zn.at(c, sn) = s;
+    float d = 0.f;
+#pragma unroll
+    for (int q = 0; q < kRtQ; ++q) {
+      const int r = lane + 32 * q;
+      if (r < n) {
+        d = fmaf(Yp[(int64_t)c * n + r], y0[q], d);
+        if (right) d = fmaf(Fp[(int64_t)c * n + r], y1[q], d);
+      }
+    }
+    d = warp_sum(d);
+    if (lane == 0) zn.at(c, sn) = zc.at(c, so) - d;
   }
 }
 
