@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(NT, 4) pair_cta(CArgs<T> a)
                       : (c < n ? C.G.at(c * mx + (r - mj), sj1) : C.o.at(r - mj, sj1));
       }
       __syncthreads();
-      ::cta::householder(A, ld, rows, n, ld, red);
+      ::cta::panel_qr<kBlocked>(A, ld, rows, n, ld, red, sh);
       const int g2 = rows < n ? rows : n;
       for (int e = tid; e < g2 * n; e += NT) {
         const int r = e / n, c = e - r * n;
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs<T> a)
         A[e] = c < n ? C.G.at(c * mx + r, sb) : C.o.at(r, sb);
       }
       __syncthreads();
-      ::cta::householder(A, ld, m0, n, ld, red);
+      ::cta::panel_qr<kBlocked>(A, ld, m0, n, ld, red, sh);
       if (tid == 0)
         for (int i = 0; i < n; ++i)
           if (A[(int64_t)i * ld + i] == T(0)) atomicOr(a.flag, 2);
@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs<T> a)
         WS[e] = c < n ? C.G.at(c * mx + r, s) : C.o.at(r, s);
       }
       __syncthreads();
-      ::cta::householder(WS, ldA, ms, n, ldA, red);
+      ::cta::panel_qr<kBlocked>(WS, ldA, ms, n, ldA, red, sh);
     }
     for (int e = tid; e < rowsT * ldT; e += NT) {
       const int r = e / ldT, c = e - r * ldT;
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs<T> a)
                      : (c < n ? WT[(int64_t)(n + r - gp) * ldT + n + c] : WT[(int64_t)(n + r - gp) * ldT + 2 * n]);
     }
     __syncthreads();
-    ::cta::householder(WF, ldF, rF, n, ldF, red);
+    ::cta::panel_qr<kBlocked>(WF, ldF, rF, n, ldF, red, sh);
     const int g2 = rF < n ? rF : n;
     for (int e = tid; e < g2 * n; e += NT) {
       const int r = e / n, c = e - r * n;
