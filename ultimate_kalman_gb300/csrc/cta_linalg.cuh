@@ -107,6 +107,91 @@ constexpr int kWyRows = 8; /* trailing-column rows loaded together */
  * scales, partial dot products (4 warps x kWyNB), look-ahead norms (4) */
 constexpr int kWyShared = kMaxPanelRows * kWyNB + kWyNB * kWyNB + 2 * kWyNB + 4 * kWyNB + 4;
 
+/* Applies the panel's reflectors H_{kb-1} .. H_0 to CW columns c, c + dc of
+ * the row-major C (rows 0..prow-1): w = V^T c, then u_b = tau_b (w_b -
+ * sum_{l<b} (v_l^T v_b) u_l), c <- c - V u.  V (unit form) and the Gram
+ * matrix are in shared memory.                                               */
+template <int CW, typename T>
+static __device__ __forceinline__ void wy_columns(T* C, int ld, int prow, int c, int dc, const T* Vs, const T* Gs,
+                                                  const T* taus, int kb)
+{
+  T w[CW][kWyNB];
+#pragma unroll
+  for (int q = 0; q < CW; ++q)
+#pragma unroll
+    for (int b = 0; b < kWyNB; ++b) w[q][b] = T(0);
+  /* rows in groups of kWyRows: their loads are in flight together */
+  int i = 0;
+#pragma unroll 1
+  for (; i + kWyRows <= prow; i += kWyRows) {
+    T cv[CW][kWyRows];
+#pragma unroll
+    for (int u = 0; u < kWyRows; ++u)
+#pragma unroll
+      for (int q = 0; q < CW; ++q) cv[q][u] = C[(int64_t)(i + u) * ld + c + q * dc];
+#pragma unroll
+    for (int u = 0; u < kWyRows; ++u)
+#pragma unroll
+      for (int b = 0; b < kWyNB; ++b) {
+        const T v = Vs[(i + u) * kWyNB + b];
+#pragma unroll
+        for (int q = 0; q < CW; ++q) w[q][b] = fma(v, cv[q][u], w[q][b]);
+      }
+  }
+#pragma unroll 1
+  for (; i < prow; ++i)
+#pragma unroll
+    for (int q = 0; q < CW; ++q) {
+      const T ci = C[(int64_t)i * ld + c + q * dc];
+#pragma unroll
+      for (int b = 0; b < kWyNB; ++b) w[q][b] = fma(Vs[i * kWyNB + b], ci, w[q][b]);
+    }
+  /* an opaque zero offset keeps the Gram matrix in shared memory instead of
+     120 loop-invariant registers */
+  int g0 = 0;
+  asm volatile("" : "+r"(g0));
+#pragma unroll
+  for (int b = 0; b < kWyNB; ++b) {
+    const T tb = b < kb ? taus[b] : T(0);
+#pragma unroll
+    for (int q = 0; q < CW; ++q) {
+      T sm = w[q][b];
+#pragma unroll
+      for (int l = 0; l < b; ++l) sm = fma(-Gs[g0 + l * kWyNB + b], w[q][l], sm);
+      w[q][b] = tb * sm; /* w now holds u */
+    }
+  }
+  i = 0;
+#pragma unroll 1
+  for (; i + kWyRows <= prow; i += kWyRows) {
+    T cv[CW][kWyRows];
+#pragma unroll
+    for (int u = 0; u < kWyRows; ++u)
+#pragma unroll
+      for (int q = 0; q < CW; ++q) cv[q][u] = C[(int64_t)(i + u) * ld + c + q * dc];
+#pragma unroll
+    for (int u = 0; u < kWyRows; ++u) {
+#pragma unroll
+      for (int b = 0; b < kWyNB; ++b) {
+        const T v = Vs[(i + u) * kWyNB + b];
+#pragma unroll
+        for (int q = 0; q < CW; ++q) cv[q][u] = fma(-v, w[q][b], cv[q][u]);
+      }
+#pragma unroll
+      for (int q = 0; q < CW; ++q) C[(int64_t)(i + u) * ld + c + q * dc] = cv[q][u];
+    }
+  }
+#pragma unroll 1
+  for (; i < prow; ++i)
+#pragma unroll
+    for (int q = 0; q < CW; ++q) {
+      T ci = C[(int64_t)i * ld + c + q * dc];
+#pragma unroll
+      for (int b = 0; b < kWyNB; ++b) ci = fma(-Vs[i * kWyNB + b], w[q][b], ci);
+      C[(int64_t)i * ld + c + q * dc] = ci;
+    }
+}
+
 template <typename T>
 static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols, T* red, T* sh)
 {
@@ -216,60 +301,10 @@ static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols
     }
     __syncthreads();
     T* C = A + (int64_t)k0 * ld; /* rows k0.. */
-    for (int c = c0 + tid; c < cols; c += NT) {
-      T w[kWyNB];
-#pragma unroll
-      for (int b = 0; b < kWyNB; ++b) w[b] = T(0);
-      /* rows in groups of kWyRows: their loads are in flight together */
-      int i = 0;
-#pragma unroll 1
-      for (; i + kWyRows <= prow; i += kWyRows) {
-        T cv[kWyRows];
-#pragma unroll
-        for (int u = 0; u < kWyRows; ++u) cv[u] = C[(int64_t)(i + u) * ld + c];
-#pragma unroll
-        for (int u = 0; u < kWyRows; ++u)
-#pragma unroll
-          for (int b = 0; b < kWyNB; ++b) w[b] = fma(Vs[(i + u) * kWyNB + b], cv[u], w[b]);
-      }
-#pragma unroll 1
-      for (; i < prow; ++i) {
-        const T ci = C[(int64_t)i * ld + c];
-#pragma unroll
-        for (int b = 0; b < kWyNB; ++b) w[b] = fma(Vs[i * kWyNB + b], ci, w[b]);
-      }
-      /* an opaque zero offset keeps the Gram matrix in shared memory instead
-         of 120 loop-invariant registers */
-      int g0 = 0;
-      asm volatile("" : "+r"(g0));
-#pragma unroll
-      for (int b = 0; b < kWyNB; ++b) {
-        T sm = w[b];
-#pragma unroll
-        for (int l = 0; l < b; ++l) sm = fma(-Gs[g0 + l * kWyNB + b], w[l], sm);
-        w[b] = taus[b < kb ? b : 0] * (b < kb ? sm : T(0)); /* w now holds u */
-      }
-      i = 0;
-#pragma unroll 1
-      for (; i + kWyRows <= prow; i += kWyRows) {
-        T cv[kWyRows];
-#pragma unroll
-        for (int u = 0; u < kWyRows; ++u) cv[u] = C[(int64_t)(i + u) * ld + c];
-#pragma unroll
-        for (int u = 0; u < kWyRows; ++u) {
-#pragma unroll
-          for (int b = 0; b < kWyNB; ++b) cv[u] = fma(-Vs[(i + u) * kWyNB + b], w[b], cv[u]);
-          C[(int64_t)(i + u) * ld + c] = cv[u];
-        }
-      }
-#pragma unroll 1
-      for (; i < prow; ++i) {
-        T ci = C[(int64_t)i * ld + c];
-#pragma unroll
-        for (int b = 0; b < kWyNB; ++b) ci = fma(-Vs[i * kWyNB + b], w[b], ci);
-        C[(int64_t)i * ld + c] = ci;
-      }
-    }
+    int c = c0 + tid;
+    if constexpr (sizeof(T) == sizeof(float)) /* two columns per thread: twice the loads in flight */
+      for (; c + NT < cols; c += 2 * NT) wy_columns<2>(C, ld, prow, c, NT, Vs, Gs, taus, kb);
+    for (; c < cols; c += NT) wy_columns<1>(C, ld, prow, c, 0, Vs, Gs, taus, kb);
     __syncthreads();
   }
 }
