@@ -58,6 +58,10 @@ enum {
 /* Number of refinement sweeps with KALMAN_GPU_FP32_REFINE (1..3; 0 selects the
  * default, 2).  Each sweep multiplies the error by about eps32 * cond(A)^2.  */
 #define KALMAN_GPU_REFINE_SWEEPS(k) (((uint32_t)(k) & 3u) << 21)
+/* With KALMAN_GPU_FP32_REFINE, at state dimensions 64..128: the blocked QR's
+ * trailing updates run on the tensor cores in 3xTF32 (split TF32 products,
+ * FP32 accumulation) instead of FP32 FMAs.  No reference counterpart.       */
+#define KALMAN_GPU_TF32X3 (1u << 23)
 
 /* Last error of the calling thread: status code and a one-line message.     */
 int         kalman_gpu_last_status(void);

@@ -2970,19 +2970,28 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
     UKG_LAUNCH(UKG_K_WEIGH, st, (ctak::weigh_cta<T><<<grid(p->nsteps), cta::NT, 0, st>>>(a, raw, p->nsteps)));
   }
   const int kPair = P.fp32 ? UKG_K_PAIR32 : UKG_K_PAIR, kSolve = P.fp32 ? UKG_K_SOLVE32 : UKG_K_SOLVE;
+  /* 3xTF32 tensor-core trailing updates in the FP32 blocked QR (an option) */
+  constexpr bool kF32 = sizeof(T) == sizeof(float);
+  const bool tc = kF32 && (options & KALMAN_GPU_TF32X3) != 0;
   for (int l = 0; l < nlev; ++l) {
     ctak::CArgs<T> a;
     common(a, l);
     a.ce = eq_level(l);
     if (l + 1 < nlev) a.ne = eq_level(l + 1);
     if (lp[l].npairs > 0) {
-      if (n >= cta::kBlockedMinN)
+      if (n >= cta::kBlockedMinN && tc) {
+        if constexpr (kF32)
+          UKG_LAUNCH(kPair, st, (ctak::pair_cta<T, true, true><<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
+      } else if (n >= cta::kBlockedMinN)
         UKG_LAUNCH(kPair, st, (ctak::pair_cta<T, true><<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
       else
         UKG_LAUNCH(kPair, st, (ctak::pair_cta<T, false><<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
     }
     if (lp[l].ntail > 0) {
-      if (n >= cta::kBlockedMinN)
+      if (n >= cta::kBlockedMinN && tc) {
+        if constexpr (kF32)
+          UKG_LAUNCH(UKG_K_TAIL, st, (ctak::tail_cta<T, true, true><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
+      } else if (n >= cta::kBlockedMinN)
         UKG_LAUNCH(UKG_K_TAIL, st, (ctak::tail_cta<T, true><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
       else
         UKG_LAUNCH(UKG_K_TAIL, st, (ctak::tail_cta<T, false><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));

@@ -29,6 +29,7 @@ KALMAN_ALGORITHM_ODDEVEN = 1 << 2
 KALMAN_ALGORITHM_ASSOCIATIVE = 1 << 3
 KALMAN_NO_COVARIANCE = 1 << 16
 KALMAN_GPU_FP32_REFINE = 1 << 20
+KALMAN_GPU_TF32X3 = 1 << 23
 KALMAN_GPU_DEVICE, KALMAN_GPU_HOST = 0, 1
 
 STATUS = {0: "OK", 1: "EINVAL", 2: "ECUDA", 3: "ENOMEM", 4: "ESINGULAR", 5: "ENODEV"}
@@ -168,12 +169,14 @@ def measure_fp32_tflops():
     return load().kalman_gpu_measure_fp32_tflops()
 
 
-def options_for(algorithm, covariance=True, fp32_refine=False, sweeps=0):
+def options_for(algorithm, covariance=True, fp32_refine=False, sweeps=0, tf32x3=False):
     o = KALMAN_ALGORITHM_ODDEVEN if algorithm == "oddeven" else KALMAN_ALGORITHM_ASSOCIATIVE
     if not covariance:
         o |= KALMAN_NO_COVARIANCE
     if fp32_refine:
         o |= KALMAN_GPU_FP32_REFINE | ((sweeps & 3) << 21)
+        if tf32x3:
+            o |= KALMAN_GPU_TF32X3
     return o
 
 
@@ -209,11 +212,12 @@ class DeviceProblem:
     def input_bytes(self):
         return sum(a.numel() * a.element_size() for a in self.arrays.values())
 
-    def smooth(self, algorithm="oddeven", covariance=True, fp32_refine=False, stream=None, check=True, sweeps=0):
+    def smooth(self, algorithm="oddeven", covariance=True, fp32_refine=False, stream=None, check=True, sweeps=0,
+               tf32x3=False):
         L = load()
         torch = self.torch
         st = stream if stream is not None else torch.cuda.current_stream()
-        opts = options_for(algorithm, covariance and self.cov is not None, fp32_refine, sweeps)
+        opts = options_for(algorithm, covariance and self.cov is not None, fp32_refine, sweeps, tf32x3)
         f = L.kalman_gpu_smooth_oddeven_packed if algorithm == "oddeven" else L.kalman_gpu_smooth_associative_packed
         status = f(opts, ctypes.byref(self.struct), ctypes.c_void_p(st.cuda_stream))
         if check:
@@ -269,13 +273,13 @@ class Plan:
             pass
 
 
-def smooth(P, algorithm="oddeven", covariance=True, fp32_refine=False, location="device", sweeps=0):
+def smooth(P, algorithm="oddeven", covariance=True, fp32_refine=False, location="device", sweeps=0, tf32x3=False):
     """Smooths a PackedProblem on the GPU; returns (states [N,n], covs [N,n,n] or None).
     location="device": inputs are copied to GPU memory first and the device
     entry point runs on them; "host": the library is handed host arrays."""
     if location == "device":
         D = DeviceProblem(P, covariance)
-        D.smooth(algorithm, covariance, fp32_refine, sweeps=sweeps)
+        D.smooth(algorithm, covariance, fp32_refine, sweeps=sweeps, tf32x3=tf32x3)
         return D.results()
     L = load()
     N, n = P.nsteps, P.n
@@ -291,7 +295,7 @@ def smooth(P, algorithm="oddeven", covariance=True, fp32_refine=False, location=
         setattr(s, f, arrs[f].ctypes.data)
     s.state = state.ctypes.data
     s.covariance = cov.ctypes.data if cov is not None else None
-    opts = options_for(algorithm, covariance, fp32_refine, sweeps)
+    opts = options_for(algorithm, covariance, fp32_refine, sweeps, tf32x3)
     f = L.kalman_gpu_smooth_oddeven_packed if algorithm == "oddeven" else L.kalman_gpu_smooth_associative_packed
     _check(f(opts, ctypes.byref(s), None))
     if cov is not None:
