@@ -2967,7 +2967,17 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
     ctak::CArgs<T> a;
     common(a, 0);
     a.ce = eq_level(0);
-    UKG_LAUNCH(UKG_K_WEIGH, st, (ctak::weigh_cta<T><<<grid(p->nsteps), cta::NT, 0, st>>>(a, raw, p->nsteps)));
+    /* the weighing needs less scratch than the pair kernel: where two of its
+       CTAs fit one slot, twice as many run (more warps on its latency) */
+    const int64_t rmax = std::max(n, p->mmax);
+    const int64_t wneed = rmax * rmax + rmax * (2 * n + 1) + rmax * cta::NT;
+    if (2 * wneed <= a.scratch_per_cta) {
+      a.scratch_per_cta /= 2;
+      const unsigned g2 = (unsigned)std::max<int64_t>(1, std::min<int64_t>(p->nsteps, 2 * (int64_t)ncta));
+      UKG_LAUNCH(UKG_K_WEIGH, st, (ctak::weigh_cta<T><<<g2, cta::NT, 0, st>>>(a, raw, p->nsteps)));
+    } else {
+      UKG_LAUNCH(UKG_K_WEIGH, st, (ctak::weigh_cta<T><<<grid(p->nsteps), cta::NT, 0, st>>>(a, raw, p->nsteps)));
+    }
   }
   const int kPair = P.fp32 ? UKG_K_PAIR32 : UKG_K_PAIR, kSolve = P.fp32 ? UKG_K_SOLVE32 : UKG_K_SOLVE;
   /* 3xTF32 tensor-core trailing updates in the FP32 blocked QR (an option) */
@@ -3024,6 +3034,12 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
       return a;
     };
     const RawDev rawd{p->H, p->F, p->c, p->K, p->G, p->o, p->C, p->K_type, p->C_type, p->obs_rows, p->mmax};
+    /* the residual's scratch (a factor and four vectors, FP64) is small: two
+       of its CTAs per slot where they fit */
+    const int64_t rr = std::max(n, p->mmax), rneed = rr * rr + 4 * rr;
+    const bool r2 = 2 * rneed <= per_cta;
+    const int64_t rper = r2 ? per_cta / 2 : per_cta;
+    const unsigned rgrid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(p->nsteps, (r2 ? 2 : 1) * (int64_t)ncta));
     for (int sw = 0; sw < sweeps; ++sw) {
       Soa<double> wE{(double*)(B + P.o_rE), P.S0}, zp{(double*)(B + P.o_rO), P.S0};
       Soa<float> z0{(float*)(B + P.o_z[0]), std::max<int64_t>(lp[0].S, 1)};
@@ -3032,7 +3048,7 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
         common(a, 0);
         a.ce = eq_level(0);
         UKG_LAUNCH(UKG_K_RESID, st,
-                   (ctak::residual_cta<<<grid(p->nsteps), cta::NT, 0, st>>>(a, raw, wE, zp, (double*)scratch, per_cta,
+                   (ctak::residual_cta<<<rgrid, cta::NT, 0, st>>>(a, raw, wE, zp, (double*)scratch, rper,
                                                                            p->nsteps)));
         Args<float, float> r = pargs(0);
         r.state = p->state;
