@@ -109,3 +109,36 @@ def test_served_results_equal_results_alone(fp32):
     for r in done:
         X, _ = native.smooth(r.problem, covariance=False, fp32_refine=fp32)
         np.testing.assert_array_equal(r.state, X)
+
+
+def test_compact_requests_expand_to_the_packed_track():
+    """A TrackSpec's packed arrays (host) have the bytes footprint() counts and
+    the layout of serving_track's problems."""
+    rng = np.random.default_rng(5)
+    spec = serve.serving_spec(50, 6, 3, rng)
+    P = spec.to_packed()
+    assert P.nsteps == 50 and P.n == 6 and P.mmax == 6
+    assert spec.nbytes() == P.nbytes()
+    assert (P.obs_rows[1:] == 3).all() and P.obs_rows[0] == 6
+    np.testing.assert_array_equal(P.F[7], spec.F.T)
+    np.testing.assert_array_equal(P.G[7][:, :3], spec.G.T)
+    r = serve.request_stream(3, 10.0, seed=2, dims=(4,), max_len=100, compact=True)
+    assert all(isinstance(x.problem, serve.TrackSpec) for x in r)
+    assert serve.footprint(r[0]) == serve.footprint(serve.Request(0, 0.0, r[0].problem.to_packed()))
+
+
+@pytest.mark.gpu
+def test_compact_requests_served_equal_packed_alone():
+    """Compact requests, expanded on the device at admission, give the results
+    of their packed tracks smoothed alone (bit-equal)."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    from ultimate_kalman_gb300 import native
+    reqs = serve.request_stream(12, 1e6, seed=13, dims=(4, 6, 12), min_len=64, max_len=3000, compact=True)
+    ex = serve.GpuExecutor()
+    srv = serve.Server(ex, hbm_budget=1 << 32)
+    done = srv.serve(reqs)
+    for r in done:
+        X, _ = native.smooth(r.problem.to_packed(), covariance=False)
+        np.testing.assert_array_equal(r.state, X)

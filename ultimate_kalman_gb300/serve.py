@@ -54,48 +54,117 @@ class Request:
 
 
 def footprint(req: Request) -> int:
-    """Device bytes a request holds while admitted: its equations, its outputs
-    and its share of the smoother's workspace (level equations and records,
-    about twice the equations' size in FP64)."""
+    """Device bytes a request holds while admitted: its equations, the batch's
+    gathered copy of them, its outputs and its share of the smoother's
+    workspace (level equations and records, about twice the equations' size in
+    FP64)."""
     P = req.problem
     eq = P.nbytes()
     out = P.nsteps * P.n * 8 * (1 + (P.n if req.covariance else 0))
-    return int(eq + out + 2 * eq)
+    return int(eq + eq + out + 2 * eq)
 
 
-def serving_track(k, n, m, rng):
+@dataclasses.dataclass
+class TrackSpec:
+    """One request of the serving form in compact form: a time-invariant track
+    ships its matrices once and its observations per step, and is expanded into
+    the packed per-step arrays on the device when admitted (a tracking service
+    receives a model and a measurement stream, not k copies of the model).
+    to_packed() gives the same arrays on the host."""
+    n: int
+    m: int
+    k: int
+    F: np.ndarray         # n x n
+    G: np.ndarray         # m x n
+    K: np.ndarray         # n x n process noise covariance
+    C: np.ndarray         # m x m observation noise covariance
+    o0: np.ndarray        # n: the square identity-weighted step-0 observation
+    o: np.ndarray         # (k-1) x m
+    ntracks: int = 1
+
+    @property
+    def nsteps(self):
+        return self.k
+
+    @property
+    def mmax(self):
+        return self.n
+
+    def nbytes(self):
+        """Bytes of the packed per-step arrays it expands into."""
+        n, k = self.n, self.k
+        return k * (8 * (4 * n * n + 2 * n + n * n) + 2 + 4)
+
+    def to_packed(self) -> pb.PackedProblem:
+        n, m, k = self.n, self.m, self.k
+        P = pb.empty_problem(n, n, [k])
+        P.H[1:] = np.eye(n)
+        P.F[1:] = self.F.T  # column-major blocks: block s holds M^T
+        P.K[1:] = self.K.T
+        P.G[0] = np.eye(n)
+        P.C[0] = np.eye(n)
+        P.o[0] = self.o0
+        P.obs_rows[0] = n
+        P.G[1:, :, :m] = self.G.T
+        P.C[1:, :m, :m] = self.C.T
+        P.o[1:, :m] = self.o
+        P.obs_rows[1:] = m
+        return P
+
+    def materialize(self, torch, device):
+        """The packed arrays of to_packed(), built on the device from the
+        compact form (only the observations cross the host link in bulk)."""
+        n, m, k = self.n, self.m, self.k
+        f64 = dict(dtype=torch.float64, device=device)
+        t = lambda a: torch.as_tensor(np.ascontiguousarray(a)).to(device, non_blocking=True)
+        eye = torch.eye(n, **f64)
+        H = torch.zeros((k, n, n), **f64)
+        H[1:] = eye
+        F = torch.zeros((k, n, n), **f64)
+        F[1:] = t(self.F.T)
+        K = torch.zeros((k, n, n), **f64)
+        K[1:] = t(self.K.T)
+        G = torch.zeros((k, n, n), **f64)
+        G[0] = eye
+        G[1:, :, :m] = t(self.G.T)
+        C = torch.zeros((k, n, n), **f64)
+        C[0] = eye
+        C[1:, :m, :m] = t(self.C.T)
+        o = torch.zeros((k, n), **f64)
+        o[0] = t(self.o0)
+        o[1:, :m] = t(self.o)
+        obs = torch.full((k,), m, dtype=torch.int32, device=device)
+        obs[0] = n
+        types = torch.full((k,), ord("C"), dtype=torch.uint8, device=device)
+        return {"H": H, "F": F, "c": torch.zeros((k, n), **f64), "K": K, "K_type": types, "G": G, "o": o,
+                "C": C, "C_type": types.clone(), "obs_rows": obs}
+
+
+def serving_spec(k, n, m, rng) -> TrackSpec:
     """One request of the serving form: F = 0.98 Q (Q random orthogonal: spectral
     radius 0.98), H = I, c = 0, SPD process and observation covariances with
     eigenvalues in [0.1, 1], G i.i.d. N(0, 1/m), a square identity-weighted
     step-0 observation, observations drawn at random (valid least-squares
     problems; their values do not change the work)."""
-    P = pb.empty_problem(n, n, [k])
     Fm = 0.98 * pb.random_orthogonal(rng, n)
     Gm = rng.standard_normal((m, n)) / np.sqrt(m)
     Kc = pb.random_spd(rng, n)
     Cc = pb.random_spd(rng, m)
-    P.H[1:] = np.eye(n)
-    P.F[1:] = Fm.T
-    P.K[1:] = Kc.T
-    P.G[0, :, :] = np.eye(n)  # column-major blocks: G[s] holds G^T
-    P.C[0] = np.eye(n)
-    P.o[0] = rng.standard_normal(n)
-    P.obs_rows[0] = n
-    Gt = np.zeros((n, n))
-    Gt[:, :m] = Gm.T
-    Ct = np.zeros((n, n))
-    Ct[:m, :m] = Cc.T
-    P.G[1:] = Gt
-    P.C[1:] = Ct
-    P.o[1:, :m] = rng.standard_normal((k - 1, m))
-    P.obs_rows[1:] = m
-    return P
+    o0 = rng.standard_normal(n)
+    o = rng.standard_normal((k - 1, m))
+    return TrackSpec(n, m, k, Fm, Gm, Kc, Cc, o0, o)
+
+
+def serving_track(k, n, m, rng) -> pb.PackedProblem:
+    """serving_spec's track as host packed arrays."""
+    return serving_spec(k, n, m, rng).to_packed()
 
 
 def request_stream(nreq, rate, seed=0, dims=(4, 6, 12, 24), min_len=64, max_len=20000, covariance=False,
-                   fp32_refine=False):
+                   fp32_refine=False, compact=False):
     """Poisson arrivals at `rate` requests/s; state dimension uniform over `dims`
-    (m = n/2); lengths log-uniform in [min_len, max_len]."""
+    (m = n/2); lengths log-uniform in [min_len, max_len].  compact=True ships
+    each request as a TrackSpec (expanded on the device at admission)."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
@@ -103,7 +172,8 @@ def request_stream(nreq, rate, seed=0, dims=(4, 6, 12, 24), min_len=64, max_len=
         t += rng.exponential(1.0 / rate)
         n = int(rng.choice(dims))
         k = int(np.floor(np.exp(rng.uniform(np.log(min_len), np.log(max_len)))))
-        out.append(Request(i, t, serving_track(k, n, n // 2, rng), covariance, fp32_refine))
+        spec = serving_spec(k, n, n // 2, rng)
+        out.append(Request(i, t, spec if compact else spec.to_packed(), covariance, fp32_refine))
     return out
 
 
@@ -118,6 +188,9 @@ class GpuExecutor:
 
     def upload(self, req: Request):
         torch = self.torch
+        if isinstance(req.problem, TrackSpec):
+            req.device = req.problem.materialize(torch, self.device)
+            return
         req.device = {f: torch.from_numpy(np.ascontiguousarray(getattr(req.problem, f))).to(self.device,
                                                                                           non_blocking=True)
                       for f in FIELDS}
@@ -130,7 +203,8 @@ class GpuExecutor:
         import ctypes
         torch, native = self.torch, self.native
         n, mmax, cov, f32 = batch[0].key()
-        arrays = {f: torch.cat([r.device[f] for r in batch]) for f in FIELDS}
+        arrays = {f: (batch[0].device[f] if len(batch) == 1 else torch.cat([r.device[f] for r in batch]))
+                  for f in FIELDS}
         lens = np.array([r.steps for r in batch], dtype=np.int64)
         ts = np.zeros(len(batch) + 1, dtype=np.int64)
         ts[1:] = np.cumsum(lens)
@@ -237,32 +311,41 @@ def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--requests", type=int, default=300)
     ap.add_argument("--loads", default="0.3,0.6,0.9", help="offered loads as fractions of the measured capacity")
+    ap.add_argument("--min-len", type=int, default=64)
     ap.add_argument("--max-len", type=int, default=20000)
     ap.add_argument("--budget-gb", type=float, default=16.0)
     ap.add_argument("--fp32-refine", action="store_true")
+    ap.add_argument("--compact", action="store_true",
+                    help="ship requests as time-invariant models + observation streams, expanded on the device")
+    ap.add_argument("--calibration", type=int, default=64, help="requests of the capacity calibration")
     ap.add_argument("--seed", type=int, default=0)
     args = ap.parse_args()
     ex = GpuExecutor()
-    # capacity: steps/s of one batch of a calibration stream served back to back
-    cal = request_stream(min(args.requests, 64), 1e9, seed=args.seed + 99, max_len=args.max_len,
-                         fp32_refine=args.fp32_refine)
+    stream = lambda nreq, rate, seed: request_stream(nreq, rate, seed=seed, min_len=args.min_len, max_len=args.max_len,
+                                                     fp32_refine=args.fp32_refine, compact=args.compact)
+    budget = args.budget_gb * 2 ** 30
+    # capacity: steps/s of a calibration stream served back to back
+    cal = stream(min(args.requests, args.calibration), 1e9, args.seed + 99)
     for r in cal:
         r.arrival = 0.0
-    srv = Server(ex, hbm_budget=args.budget_gb * 2 ** 30)
-    srv.serve(cal[:8])  # warm-up
+    Server(ex, hbm_budget=budget).serve(cal[:8])  # warm-up
     t0 = time.perf_counter()
-    done = Server(ex, hbm_budget=args.budget_gb * 2 ** 30).serve(cal)
+    done = Server(ex, hbm_budget=budget).serve(cal)
     cap_steps = sum(r.steps for r in done) / (time.perf_counter() - t0)
-    mean_steps = np.mean([r.steps for r in cal])
+    # request rate at capacity, from the length distribution's mean (log-uniform:
+    # (max - min) / ln(max / min)), so that a load is a fraction of capacity in steps/s
+    mean_steps = (args.max_len - args.min_len) / np.log(args.max_len / args.min_len)
     cap_rate = cap_steps / mean_steps
-    out = {"capacity_steps_per_s": cap_steps, "capacity_requests_per_s": cap_rate, "loads": []}
+    out = {"capacity_steps_per_s": cap_steps, "capacity_requests_per_s": cap_rate,
+           "lengths": [args.min_len, args.max_len], "compact": args.compact, "budget_gb": args.budget_gb, "loads": []}
     for load in [float(x) for x in args.loads.split(",")]:
-        reqs = request_stream(args.requests, load * cap_rate, seed=args.seed, max_len=args.max_len,
-                              fp32_refine=args.fp32_refine)
-        srv = Server(ex, hbm_budget=args.budget_gb * 2 ** 30)
+        reqs = stream(args.requests, load * cap_rate, args.seed)
+        srv = Server(ex, hbm_budget=budget)
         done = srv.serve(reqs)
         s = summarize(done)
+        span = max(r.arrival for r in reqs) - min(r.arrival for r in reqs)
         s.update({"offered_load": load, "arrival_rate_per_s": load * cap_rate,
+                  "realized_load": float(sum(r.steps for r in reqs) / span / cap_steps) if span > 0 else None,
                   "batches": len(srv.batches), "mean_batch_requests": float(np.mean([b[1] for b in srv.batches])),
                   "peak_hbm_gb": srv.peak_in_use / 2 ** 30})
         out["loads"].append(s)
