@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-large", action="store_true", help="skip the n=128 large-state line")
     ap.add_argument("--fp32-only", action="store_true",
                     help="time the precision form only (no plain FP64 pass, probes, e2e or CPU leg): profiling runs")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -328,10 +329,50 @@ def run_gpu(args):
                                 "sample": f"first {ntr} of {P.ntracks} tracks ({nsteps} steps), {dt:.1f} s, "
                                           f"oracle/kalman_oracle.c odd-even, FP64, states only, OpenMP over tracks",
                                 "rel_err_of_gpu_states_on_sample": err_o}
+    if rank == 0 and world == 1 and not args.no_large:
+        if not args.no_e2e:
+            del pin, st_h, s
+        torch.cuda.empty_cache()
+        line["large_state"] = large_state(stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def large_state(stream):
+    """The large-state shape beside the headline: one n=128, m=64, k=20,000
+    track (F = 0.995 Q, G ~ N(0, 1/m), noise covariance eigenvalues
+    log-uniform in [1e-3, 1], 5 % of steps unobserved), odd-even smoother,
+    states: the precision form (FP32 blocked QR + one FP64-residual sweep),
+    the same with 3xTF32 tensor-core updates, and plain FP64."""
+    import torch
+    from ultimate_kalman_gb300 import native, shapes
+    P = shapes.synthetic_track(20000, 128, 64, rho=0.995, lo=1e-3, log_cov=True)
+    D = native.DeviceProblem(P, covariance=False)
+    kw32 = dict(covariance=False, fp32_refine=True, sweeps=1)
+    kwtc = dict(kw32, tf32x3=True)
+    D.smooth("oddeven", **kw32)
+    ms32, _ = time_smooths(D, 3, stream, **kw32)
+    X32 = D.state.clone()
+    D.smooth("oddeven", **kwtc)
+    mstc, _ = time_smooths(D, 2, stream, **kwtc)
+    Xtc = D.state.clone()
+    D.smooth("oddeven", covariance=False)
+    ms64, _ = time_smooths(D, 2, stream, covariance=False)
+    X64 = D.state
+    rel = lambda X: float(((X - X64).abs().amax(dim=1) / X64.abs().amax(dim=1)).max().item())
+    out = {"what": "single track n=128, m=64, k=20000, odd-even, states; F = 0.995 Q, G ~ N(0, 1/m), noise "
+                   "covariance eigenvalues log-uniform in [1e-3, 1], 5 % of steps unobserved; synthetic",
+           "fp32_refine": {"ms": ms32, "steps_per_s": P.nsteps / (ms32 * 1e-3), "rel_err_vs_fp64": rel(X32),
+                           "form": "FP32 blocked QR (FMA updates) + 1 FP64-residual sweep"},
+           "tf32x3": {"ms": mstc, "steps_per_s": P.nsteps / (mstc * 1e-3), "rel_err_vs_fp64": rel(Xtc),
+                      "form": "FP32 blocked QR, 3xTF32 tensor-core updates + 1 FP64-residual sweep"},
+           "plain_fp64": {"ms": ms64, "steps_per_s": P.nsteps / (ms64 * 1e-3)},
+           "speedup_fp32_refine_vs_fp64": ms64 / ms32}
+    del D
+    torch.cuda.empty_cache()
+    return out
 
 
 def main():
