@@ -111,6 +111,34 @@ int kalman_gpu_smooth_associative_packed(uint32_t options, const kalman_gpu_prob
 int kalman_gpu_smooth_tracks(uint32_t options, kalman_step_equations_t** equations,
                              const kalman_step_index_t* track_lengths, int32_t ntracks);
 
+/* Device-side equation builder for tracks whose model does not change along
+ * the track (no reference counterpart: it stands in for the kalman_evolve /
+ * kalman_observe loop of c/kalman_explicit_representation.c:164-244, which
+ * builds every step's matrices on the host).  Fills steps first .. first+k-1
+ * of the packed DEVICE arrays that p points to (H, F, c, K, K_type, G, o, C,
+ * C_type, obs_rows; step `first` is the track's step 0):
+ *   step 0:        no evolution (H, F, c, K zero, K_type 'C'); the observation
+ *                  G0 (m0 x n), o0 (m0), C0 (m0 x m0, type C0_type);
+ *   steps 1..k-1:  the evolution H, F (n x n), c (n), K (n x n, type K_type);
+ *                  the observation G (m x n), C (m x m, type C_type) and
+ *                  o + (i-1)*ldo (m entries), with obs_rows[i-1] rows (NULL:
+ *                  m at every step; 0 marks a missing observation).
+ * Model matrices are column-major with ld = rows, in device memory; unused
+ * rows of the packed G, o, C are zero.  m0, m <= p->mmax.  Queued on
+ * cuda_stream; returns a status code.                                       */
+typedef struct kalman_gpu_invariant_model_st {
+  int32_t m0, m;
+  const double *H, *F, *c, *K;
+  char K_type;
+  const double *G0, *o0, *C0;
+  char C0_type;
+  const double *G, *C;
+  char C_type;
+} kalman_gpu_invariant_model_t;
+int kalman_gpu_expand_invariant(const kalman_gpu_problem_t* p, int64_t first, int64_t k,
+                                const kalman_gpu_invariant_model_t* model, const double* o, int64_t ldo,
+                                const int32_t* obs_rows, void* cuda_stream);
+
 /* Kernel timing.  While enabled (per host thread), each kernel launch of the
  * smoothers is bracketed by CUDA events on its stream.  _read returns, per
  * kernel class that ran since it was enabled, its name, summed time (ms) and

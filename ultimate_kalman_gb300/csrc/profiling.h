@@ -18,6 +18,7 @@ enum {
   UKG_K_RESID,
   UKG_K_RT,
   UKG_K_RSOLVE,
+  UKG_K_BUILD,
   UKG_K_COUNT
 };
 

@@ -68,6 +68,18 @@ class ProblemStruct(ctypes.Structure):
     ]
 
 
+class InvariantModel(ctypes.Structure):
+    """kalman_gpu_invariant_model_t (include/kalman_gpu.h): device pointers to
+    column-major model matrices."""
+    _fields_ = [
+        ("m0", ctypes.c_int32), ("m", ctypes.c_int32),
+        ("H", ctypes.c_void_p), ("F", ctypes.c_void_p), ("c", ctypes.c_void_p), ("K", ctypes.c_void_p),
+        ("K_type", ctypes.c_char),
+        ("G0", ctypes.c_void_p), ("o0", ctypes.c_void_p), ("C0", ctypes.c_void_p), ("C0_type", ctypes.c_char),
+        ("G", ctypes.c_void_p), ("C", ctypes.c_void_p), ("C_type", ctypes.c_char),
+    ]
+
+
 # every symbol include/*.h declares (checked by tests/test_abi.py)
 EXPORTED = [
     "kalman_covariance_matrix_weigh", "kalman_covariance_matrix_explicit", "kalman_create", "kalman_create_options",
@@ -87,6 +99,7 @@ EXPORTED = [
     "kalman_gpu_release", "kalman_gpu_profile_enable", "kalman_gpu_profile_read", "kalman_gpu_launch_count",
     "kalman_gpu_measure_fp64_tflops", "kalman_gpu_measure_fp32_tflops", "kalman_gpu_smooth_oddeven_noalloc",
     "kalman_gpu_plan_create", "kalman_gpu_plan_execute", "kalman_gpu_plan_status", "kalman_gpu_plan_destroy",
+    "kalman_gpu_expand_invariant",
 ]
 
 _lib = None
@@ -128,6 +141,9 @@ def load(path=LIB_PATH):
     L.kalman_gpu_plan_status.argtypes = [ctypes.c_void_p]
     L.kalman_gpu_plan_status.restype = ctypes.c_int
     L.kalman_gpu_plan_destroy.argtypes = [ctypes.c_void_p]
+    L.kalman_gpu_expand_invariant.argtypes = [P, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(InvariantModel),
+                                              ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
+    L.kalman_gpu_expand_invariant.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -412,3 +428,13 @@ def smooth_struct(algorithm, s, covariance=True, fp32_refine=False, stream=None,
     opts = options_for(algorithm, covariance, fp32_refine, sweeps)
     f = L.kalman_gpu_smooth_oddeven_packed if algorithm == "oddeven" else L.kalman_gpu_smooth_associative_packed
     _check(f(opts, ctypes.byref(s), ctypes.c_void_p(stream.cuda_stream) if stream is not None else None))
+
+
+def expand_invariant(s, first, k, model, o, ldo, obs_rows=None, stream=None):
+    """kalman_gpu_expand_invariant on the device arrays of ProblemStruct s:
+    steps first .. first+k-1 from the InvariantModel and the observation
+    stream o (a device pointer, ldo doubles per step).  Raises on failure."""
+    L = load()
+    st = stream.cuda_stream if stream is not None and hasattr(stream, "cuda_stream") else stream
+    _check(L.kalman_gpu_expand_invariant(ctypes.byref(s), int(first), int(k), ctypes.byref(model),
+                                         ctypes.c_void_p(o), int(ldo), ctypes.c_void_p(obs_rows), ctypes.c_void_p(st)))

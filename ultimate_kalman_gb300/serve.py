@@ -112,32 +112,32 @@ class TrackSpec:
         return P
 
     def materialize(self, torch, device):
-        """The packed arrays of to_packed(), built on the device from the
-        compact form (only the observations cross the host link in bulk)."""
+        """The packed arrays of to_packed(), built on the device by the
+        library's equation builder (kalman_gpu_expand_invariant): only the
+        model and the observations cross the host link."""
+        from . import native
         n, m, k = self.n, self.m, self.k
         f64 = dict(dtype=torch.float64, device=device)
-        t = lambda a: torch.as_tensor(np.ascontiguousarray(a)).to(device, non_blocking=True)
-        eye = torch.eye(n, **f64)
-        H = torch.zeros((k, n, n), **f64)
-        H[1:] = eye
-        F = torch.zeros((k, n, n), **f64)
-        F[1:] = t(self.F.T)
-        K = torch.zeros((k, n, n), **f64)
-        K[1:] = t(self.K.T)
-        G = torch.zeros((k, n, n), **f64)
-        G[0] = eye
-        G[1:, :, :m] = t(self.G.T)
-        C = torch.zeros((k, n, n), **f64)
-        C[0] = eye
-        C[1:, :m, :m] = t(self.C.T)
-        o = torch.zeros((k, n), **f64)
-        o[0] = t(self.o0)
-        o[1:, :m] = t(self.o)
-        obs = torch.full((k,), m, dtype=torch.int32, device=device)
-        obs[0] = n
-        types = torch.full((k,), ord("C"), dtype=torch.uint8, device=device)
-        return {"H": H, "F": F, "c": torch.zeros((k, n), **f64), "K": K, "K_type": types, "G": G, "o": o,
-                "C": C, "C_type": types.clone(), "obs_rows": obs}
+        arrays = {"H": torch.empty((k, n, n), **f64), "F": torch.empty((k, n, n), **f64),
+                  "c": torch.empty((k, n), **f64), "K": torch.empty((k, n, n), **f64),
+                  "K_type": torch.empty(k, dtype=torch.uint8, device=device), "G": torch.empty((k, n, n), **f64),
+                  "o": torch.empty((k, n), **f64), "C": torch.empty((k, n, n), **f64),
+                  "C_type": torch.empty(k, dtype=torch.uint8, device=device),
+                  "obs_rows": torch.empty(k, dtype=torch.int32, device=device)}
+        s = native.ProblemStruct()
+        s.n, s.mmax, s.ntracks, s.location, s.nsteps = n, n, 1, native.KALMAN_GPU_DEVICE, k
+        for f, a in arrays.items():
+            setattr(s, f, a.data_ptr())
+        dev = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64)).to(device)
+        eye = dev(np.eye(n))
+        # column-major device copies: the row-major memory of M^T
+        F, K, G, C, c = dev(self.F.T), dev(self.K.T), dev(self.G.T), dev(self.C.T), dev(np.zeros(n))
+        o0, o = dev(self.o0), dev(self.o if k > 1 else np.zeros((1, m)))
+        md = native.InvariantModel(m0=n, m=m, H=eye.data_ptr(), F=F.data_ptr(), c=c.data_ptr(), K=K.data_ptr(),
+                                   K_type=b"C", G0=eye.data_ptr(), o0=o0.data_ptr(), C0=eye.data_ptr(), C0_type=b"C",
+                                   G=G.data_ptr(), C=C.data_ptr(), C_type=b"C")
+        native.expand_invariant(s, 0, k, md, o.data_ptr(), m, None, torch.cuda.current_stream())
+        return arrays
 
 
 def serving_spec(k, n, m, rng) -> TrackSpec:
