@@ -103,7 +103,7 @@ def test_larger_states_cta_path(n, k):
     assert oracle.rel_err_covs(S, So) < TOL
 
 
-def test_config1_shape_n48_covariance_types():
+def test_n48_m24_covariance_types():
     """n = 48, m = 24 (the associative benchmark shape) with the 'W' and 'w'
     covariance forms."""
     P = pb.random_dynamics([33, 4], 48, 24, seed=77, per_step=True, K_type="W", C_type="w", missing=0.05)

@@ -144,7 +144,7 @@ def test_larger_states_cta_path(n, k):
     check(P, X, S)
 
 
-def test_config4_shape_n128():
+def test_n128_m64_log_uniform_covariances():
     """n = 128, m = 64 (the largest shape this build accepts), all covariance
     types of the reference in one problem."""
     P = pb.random_dynamics([23, 6], 128, 64, seed=21, per_step=True, K_type="W", C_type="F")

@@ -1,8 +1,8 @@
 """Times one smoothing of a single synthetic track of a given shape on the GPU
-(the larger-state configurations: n=48/m=24 for the associative smoother,
+(the larger-state workloads: n=48/m=24 for the associative smoother,
 n=128/m=64 for the odd-even smoother, n in {4, 6, 12, 24} for serving).
 
-The track follows the configurations' recipe: F = rho Q (Q random orthogonal),
+The track follows the large-state workloads' recipe: F = rho Q (Q random orthogonal),
 H = I, G i.i.d. N(0, 1/m), SPD noise covariances with eigenvalues in [lo, hi]
 (log-uniform with --log-cov), a square step-0 observation, a fraction of
 steps without observation.  Matrices are shared along the track (the work does
