@@ -105,3 +105,14 @@ def test_bad_ranges_are_refused():
     md = native.InvariantModel(m0=0, m=0, K_type=b"C", C0_type=b"C", C_type=b"C")
     with pytest.raises(native.KalmanError):
         native.expand_invariant(s, 8, 5, md, 0, 1)  # past the problem's steps
+
+
+def test_device_built_track_equals_the_host_built_track():
+    """shapes.device_track (the builder) and shapes.synthetic_track (host
+    numpy) give the same packed arrays for the same seed."""
+    torch = _cuda()
+    from ultimate_kalman_gb300 import shapes
+    P = shapes.synthetic_track(300, 10, 5, seed=3)
+    D = shapes.device_track(300, 10, 5, seed=3)
+    for f in FIELDS:
+        np.testing.assert_array_equal(D.arrays[f].cpu().numpy(), getattr(P, f), err_msg=f)

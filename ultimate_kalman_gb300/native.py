@@ -209,15 +209,28 @@ class DeviceProblem:
 
     def __init__(self, P, covariance=True, device="cuda"):
         import torch
-        self.P = P
+        arrays = {f: torch.from_numpy(np.ascontiguousarray(getattr(P, f))).to(device) for f in _FIELDS}
+        self._setup(P.n, P.mmax, P.track_start, arrays, covariance, device)
+
+    @classmethod
+    def from_arrays(cls, n, mmax, track_start, arrays, covariance=True, device="cuda"):
+        """A device problem over packed arrays already in GPU memory (torch
+        tensors, e.g. written by expand_invariant)."""
+        self = cls.__new__(cls)
+        self._setup(n, mmax, track_start, arrays, covariance, device)
+        return self
+
+    def _setup(self, n, mmax, track_start, arrays, covariance, device):
+        import torch
         self.torch = torch
-        self.arrays = {f: torch.from_numpy(np.ascontiguousarray(getattr(P, f))).to(device) for f in _FIELDS}
-        self.state = torch.empty((P.nsteps, P.n), dtype=torch.float64, device=device)
-        self.cov = torch.empty((P.nsteps, P.n, P.n), dtype=torch.float64, device=device) if covariance else None
-        self.track_start = np.ascontiguousarray(P.track_start, dtype=np.int64)
+        self.arrays = arrays
+        self.track_start = np.ascontiguousarray(track_start, dtype=np.int64)
+        nsteps = int(self.track_start[-1])
+        self.state = torch.empty((nsteps, n), dtype=torch.float64, device=device)
+        self.cov = torch.empty((nsteps, n, n), dtype=torch.float64, device=device) if covariance else None
         s = ProblemStruct()
-        s.n, s.mmax, s.ntracks, s.location = P.n, P.mmax, P.ntracks, KALMAN_GPU_DEVICE
-        s.nsteps = P.nsteps
+        s.n, s.mmax, s.ntracks, s.location = n, mmax, len(self.track_start) - 1, KALMAN_GPU_DEVICE
+        s.nsteps = nsteps
         s.track_start = self.track_start.ctypes.data
         for f in _FIELDS:
             setattr(s, f, self.arrays[f].data_ptr())
