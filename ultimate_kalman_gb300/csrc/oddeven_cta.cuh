@@ -371,14 +371,17 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs<T> a)
  *   S_j = R^{-1} (I + W B^T) R^{-T}
  * Scratch (row-major): R, B (n x 2n), W (n x 2n), M, X (n x n each), x.
  * ------------------------------------------------------------------------ */
+constexpr int kSigmaCols = 16; /* columns of Sigma staged in shared memory at a time */
+
 template <typename T>
 __global__ void __launch_bounds__(NT) solve_cta(CArgs<T> a, int want_cov)
 {
+  __shared__ T Sq[kSigmaCols][2 * kMaxCov]; /* Sigma(:, q0 .. q0 + 15), column by column */
   const int n = a.n, tid = threadIdx.x;
   const int64_t nn = (int64_t)n * n;
   T* R = a.scratch + (int64_t)blockIdx.x * a.scratch_per_cta;
-  T* Bm = R + nn;       /* n x 2n */
-  T* W = Bm + 2 * nn;   /* n x 2n */
+  T* Bt = R + nn;       /* B^T = [F~ | Y]^T, 2n x n: Bt[k * n + r] = B(r, k) */
+  T* W = Bt + 2 * nn;   /* n x 2n, row-major */
   T* M = W + 2 * nn;    /* n x n */
   T* X = M + nn;        /* n x n */
   T* xv = X + nn;       /* n */
@@ -390,20 +393,20 @@ __global__ void __launch_bounds__(NT) solve_cta(CArgs<T> a, int want_cov)
     const int64_t oj = orig_step(a.track_start, a.level, t, j);
     const int64_t om = hp ? orig_step(a.track_start, a.level, t, j - 1) : 0;
     const int64_t op = hn ? orig_step(a.track_start, a.level, t, j + 1) : 0;
-    for (int e = tid; e < n * n; e += NT) {
+    for (int e = tid; e < n * n; e += NT) { /* records are column-major: contiguous copies */
       const int r = e / n, c = e - r * n;
       R[e] = Rr.R.at(c * n + r, item);
-      Bm[(int64_t)r * 2 * n + c] = hp ? Rr.Ft.at(c * n + r, item) : T(0);
-      Bm[(int64_t)r * 2 * n + n + c] = hn ? Rr.Y.at(c * n + r, item) : T(0);
+      Bt[e] = hp ? Rr.Ft.at(e, item) : T(0);
+      Bt[nn + e] = hn ? Rr.Y.at(e, item) : T(0);
     }
     __syncthreads();
     /* state */
     for (int r = tid; r < n; r += NT) {
       T s = a.yrhs.p ? a.yrhs.at(r, item) : Rr.rhs.at(r, item);
       if (hp)
-        for (int k = 0; k < n; ++k) s = fma(-Bm[(int64_t)r * 2 * n + k], ukg_df::narrow<T>(a.state[om * n + k]), s);
+        for (int k = 0; k < n; ++k) s = fma(-Bt[(int64_t)k * n + r], ukg_df::narrow<T>(a.state[om * n + k]), s);
       if (hn)
-        for (int k = 0; k < n; ++k) s = fma(-Bm[(int64_t)r * 2 * n + n + k], ukg_df::narrow<T>(a.state[op * n + k]), s);
+        for (int k = 0; k < n; ++k) s = fma(-Bt[nn + (int64_t)k * n + r], ukg_df::narrow<T>(a.state[op * n + k]), s);
       xv[r] = s;
     }
     __syncthreads();
@@ -416,25 +419,41 @@ __global__ void __launch_bounds__(NT) solve_cta(CArgs<T> a, int want_cov)
       __syncthreads();
       continue;
     }
-    /* W = B Sigma, one thread per row of W; Sigma entries are shared reads */
+    /* W = B Sigma over the neighbours' covariance blocks, Sigma staged in
+       shared memory kSigmaCols columns at a time (read along its columns),
+       outputs one per thread with consecutive threads on consecutive rows */
     const double* Smm = hp ? a.cov + om * nn : nullptr;
     const double* Spp = hn ? a.cov + op * nn : nullptr;
     const int64_t smp = (hp && hn) ? a.nt.slot[t] + (j + 1) / 2 : 0;
     auto sigma = [&](int k, int q) -> T { /* Sigma(k, q), 0 <= k, q < 2n */
       if (k < n) {
-        if (q < n) return hp ? Smm[(int64_t)q * n + k] : T(0);
+        if (q < n) return hp ? T(Smm[(int64_t)q * n + k]) : T(0);
         return (hp && hn) ? a.nr.U.at((q - n) * n + k, smp) : T(0); /* Smp(k, q-n) */
       }
       if (q < n) return (hp && hn) ? a.nr.U.at((k - n) * n + q, smp) : T(0); /* Smp(q, k-n) */
-      return hn ? Spp[(int64_t)(q - n) * n + (k - n)] : T(0);
+      return hn ? T(Spp[(int64_t)(q - n) * n + (k - n)]) : T(0);
     };
-    const int k0 = hp ? 0 : n, k1 = hn ? 2 * n : n;
-    for (int r = tid; r < n; r += NT)
-      for (int q = k0; q < k1; ++q) {
-        T s = T(0);
-        for (int k = k0; k < k1; ++k) s = fma(Bm[(int64_t)r * 2 * n + k], sigma(k, q), s);
-        W[(int64_t)r * 2 * n + q] = s;
+    const int k0 = hp ? 0 : n, k1 = hn ? 2 * n : n, kw = k1 - k0;
+    for (int q0 = k0; q0 < k1; q0 += kSigmaCols) {
+      const int qn = k1 - q0 < kSigmaCols ? k1 - q0 : kSigmaCols;
+      for (int e = tid; e < qn * kw; e += NT) {
+        const int qi = e / kw, k = k0 + (e - qi * kw);
+        Sq[qi][k] = sigma(k, q0 + qi);
       }
+      __syncthreads();
+      for (int e = tid; e < qn * n; e += NT) {
+        const int qi = e / n, r = e - qi * n;
+        T s0 = T(0), s1 = T(0);
+        int k = k0;
+        for (; k + 1 < k1; k += 2) {
+          s0 = fma(Bt[(int64_t)k * n + r], Sq[qi][k], s0);
+          s1 = fma(Bt[(int64_t)(k + 1) * n + r], Sq[qi][k + 1], s1);
+        }
+        if (k < k1) s0 = fma(Bt[(int64_t)k * n + r], Sq[qi][k], s0);
+        W[(int64_t)r * 2 * n + q0 + qi] = s0 + s1;
+      }
+      __syncthreads();
+    }
     for (int r = tid; r < n; r += NT)
       for (int q = 0; q < 2 * n; ++q)
         if (q < k0 || q >= k1) W[(int64_t)r * 2 * n + q] = T(0);
@@ -442,9 +461,14 @@ __global__ void __launch_bounds__(NT) solve_cta(CArgs<T> a, int want_cov)
     /* M = I + W B^T */
     for (int e = tid; e < n * n; e += NT) {
       const int r = e / n, c = e - r * n;
-      T s = r == c ? T(1) : T(0);
-      for (int q = k0; q < k1; ++q) s = fma(W[(int64_t)r * 2 * n + q], Bm[(int64_t)c * 2 * n + q], s);
-      M[e] = s;
+      T s0 = r == c ? T(1) : T(0), s1 = T(0);
+      int q = k0;
+      for (; q + 1 < k1; q += 2) {
+        s0 = fma(W[(int64_t)r * 2 * n + q], Bt[(int64_t)q * n + c], s0);
+        s1 = fma(W[(int64_t)r * 2 * n + q + 1], Bt[(int64_t)(q + 1) * n + c], s1);
+      }
+      if (q < k1) s0 = fma(W[(int64_t)r * 2 * n + q], Bt[(int64_t)q * n + c], s0);
+      M[e] = s0 + s1;
     }
     __syncthreads();
     if (a.level > 0) { /* off-diagonal blocks: -R^{-1} W */
