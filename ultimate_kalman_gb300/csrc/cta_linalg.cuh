@@ -619,42 +619,71 @@ static __device__ bool cholesky_cm(T* L, int rows)
   return ok;
 }
 
+/* B <- L^{-1} B for CW columns c, c + dc of the row-major B (rows x cols,
+ * ldb) and the lower triangular, column-major L (ld rows), four rows at a
+ * time: each L entry loaded once per CW columns, each B entry once per four
+ * rows, 4 CW independent chains.                                            */
+template <int CW, typename T>
+static __device__ __forceinline__ void fsub_cols(const T* L, int rows, T* B, int ldb, int c, int dc)
+{
+  for (int i0 = 0; i0 < rows; i0 += 4) {
+    const int nq = rows - i0 < 4 ? rows - i0 : 4;
+    T s[CW][4];
+#pragma unroll
+    for (int w = 0; w < CW; ++w)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) s[w][q] = q < nq ? B[(int64_t)(i0 + q) * ldb + c + w * dc] : T(0);
+    if (nq == 4) {
+#pragma unroll 2
+      for (int k = 0; k < i0; ++k) {
+        T bk[CW];
+#pragma unroll
+        for (int w = 0; w < CW; ++w) bk[w] = B[(int64_t)k * ldb + c + w * dc];
+        const T* Lk = L + (int64_t)k * rows + i0;
+        const T l0 = Lk[0], l1 = Lk[1], l2 = Lk[2], l3 = Lk[3];
+#pragma unroll
+        for (int w = 0; w < CW; ++w) {
+          s[w][0] = fma(-l0, bk[w], s[w][0]);
+          s[w][1] = fma(-l1, bk[w], s[w][1]);
+          s[w][2] = fma(-l2, bk[w], s[w][2]);
+          s[w][3] = fma(-l3, bk[w], s[w][3]);
+        }
+      }
+    } else {
+      for (int k = 0; k < i0; ++k) {
+#pragma unroll
+        for (int w = 0; w < CW; ++w) {
+          const T bk = B[(int64_t)k * ldb + c + w * dc];
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (q < nq) s[w][q] = fma(-L[(int64_t)k * rows + i0 + q], bk, s[w][q]);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (q < nq) {
+        const T dq = L[(int64_t)(i0 + q) * rows + i0 + q];
+#pragma unroll
+        for (int w = 0; w < CW; ++w) {
+#pragma unroll
+          for (int r = 0; r < q; ++r) s[w][q] = fma(-L[(int64_t)(i0 + r) * rows + i0 + q], s[w][r], s[w][q]);
+          s[w][q] /= dq;
+          B[(int64_t)(i0 + q) * ldb + c + w * dc] = s[w][q];
+        }
+      }
+  }
+}
+
 /* B <- L^{-1} B for the row-major B (rows x cols, ldb) and the lower
- * triangular, column-major L (ld rows): one thread per column, four rows at a
- * time (each B entry loaded once per four rows, four independent chains).   */
+ * triangular, column-major L (ld rows): one thread per column (two where the
+ * columns go past the CTA's threads), four rows at a time.                 */
 template <typename T>
 static __device__ void forward_subst_cm(const T* L, int rows, T* B, int ldb, int cols)
 {
-  for (int c = threadIdx.x; c < cols; c += NT)
-    for (int i0 = 0; i0 < rows; i0 += 4) {
-      const int nq = rows - i0 < 4 ? rows - i0 : 4;
-      T s[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) s[q] = q < nq ? B[(int64_t)(i0 + q) * ldb + c] : T(0);
-      if (nq == 4) {
-        for (int k = 0; k < i0; ++k) {
-          const T bk = B[(int64_t)k * ldb + c];
-          const T* Lk = L + (int64_t)k * rows + i0;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) s[q] = fma(-Lk[q], bk, s[q]);
-        }
-      } else {
-        for (int k = 0; k < i0; ++k) {
-          const T bk = B[(int64_t)k * ldb + c];
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-            if (q < nq) s[q] = fma(-L[(int64_t)k * rows + i0 + q], bk, s[q]);
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (q < nq) {
-#pragma unroll
-          for (int r = 0; r < q; ++r) s[q] = fma(-L[(int64_t)(i0 + r) * rows + i0 + q], s[r], s[q]);
-          s[q] /= L[(int64_t)(i0 + q) * rows + i0 + q];
-          B[(int64_t)(i0 + q) * ldb + c] = s[q];
-        }
-    }
+  int c = threadIdx.x;
+  for (; c + NT < cols; c += 2 * NT) fsub_cols<2>(L, rows, B, ldb, c, NT);
+  for (; c < cols; c += NT) fsub_cols<1>(L, rows, B, ldb, c, 0);
   __syncthreads();
 }
 
