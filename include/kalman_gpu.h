@@ -111,6 +111,17 @@ int kalman_gpu_smooth_associative_packed(uint32_t options, const kalman_gpu_prob
 int kalman_gpu_smooth_tracks(uint32_t options, kalman_step_equations_t** equations,
                              const kalman_step_index_t* track_lengths, int32_t ntracks);
 
+/* Filtered estimates (the sequential UltimateKalman filter of
+ * c/kalman_ultimate.c: evolve 140-330, observe 332-470, estimate 472-557) for
+ * every step of every track of a packed problem with DEVICE arrays: state[s]
+ * = x_{s|s} and, unless KALMAN_NO_COVARIANCE, covariance[s] = P_{s|s}
+ * (column-major), from the equations of the track's steps up to s.  Steps
+ * whose state is not yet determined get NaN and the call returns
+ * KALMAN_GPU_ESINGULAR.  Tracks run in parallel, steps in sequence.  n and
+ * mmax <= 128.  Returns when the results are in place.  No counterpart in the
+ * reference's ABI (its filter runs one step per kalman_evolve/observe call). */
+int kalman_gpu_filter_packed(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream);
+
 /* Device-side equation builder for tracks whose model does not change along
  * the track (no reference counterpart: it stands in for the kalman_evolve /
  * kalman_observe loop of c/kalman_explicit_representation.c:164-244, which

@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libukgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["oddeven.cu", "associative.cu", "builder.cu", "profiling.cu", "host_api.cpp", "matrix_ops.c"]
+SOURCES = ["oddeven.cu", "associative.cu", "builder.cu", "filter.cu", "profiling.cu", "host_api.cpp", "matrix_ops.c"]
 
 
 def nvcc():

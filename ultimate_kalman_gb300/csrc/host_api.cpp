@@ -287,6 +287,7 @@ extern "C" void kalman_gpu_release(void)
 {
   ukg_release_oddeven_workspace();
   ukg_release_associative_workspace();
+  ukg_release_filter_workspace();
   stage_release(tl_stage);
 }
 

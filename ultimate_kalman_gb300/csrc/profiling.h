@@ -19,6 +19,7 @@ enum {
   UKG_K_RT,
   UKG_K_RSOLVE,
   UKG_K_BUILD,
+  UKG_K_FILTER,
   UKG_K_COUNT
 };
 

@@ -24,6 +24,9 @@ void ukg_clear_error(void);
 int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream);
 int ukg_associative_device(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream);
 
+/* frees the filter's cached device workspace (filter.cu) */
+void ukg_release_filter_workspace(void);
+
 /* checks the arguments of a packed problem that do not need device access   */
 int ukg_validate_problem(const kalman_gpu_problem_t* p, int need_cov);
 

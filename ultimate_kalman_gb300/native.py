@@ -31,6 +31,7 @@ KALMAN_NO_COVARIANCE = 1 << 16
 KALMAN_GPU_FP32_REFINE = 1 << 20
 KALMAN_GPU_TF32X3 = 1 << 23
 KALMAN_GPU_DEVICE, KALMAN_GPU_HOST = 0, 1
+KALMAN_GPU_OK, KALMAN_GPU_EINVAL, KALMAN_GPU_ECUDA, KALMAN_GPU_ENOMEM, KALMAN_GPU_ESINGULAR, KALMAN_GPU_ENODEV = range(6)
 
 STATUS = {0: "OK", 1: "EINVAL", 2: "ECUDA", 3: "ENOMEM", 4: "ESINGULAR", 5: "ENODEV"}
 
@@ -99,7 +100,7 @@ EXPORTED = [
     "kalman_gpu_release", "kalman_gpu_profile_enable", "kalman_gpu_profile_read", "kalman_gpu_launch_count",
     "kalman_gpu_measure_fp64_tflops", "kalman_gpu_measure_fp32_tflops", "kalman_gpu_smooth_oddeven_noalloc",
     "kalman_gpu_plan_create", "kalman_gpu_plan_execute", "kalman_gpu_plan_status", "kalman_gpu_plan_destroy",
-    "kalman_gpu_expand_invariant",
+    "kalman_gpu_expand_invariant", "kalman_gpu_filter_packed",
 ]
 
 _lib = None
@@ -115,7 +116,7 @@ def load(path=LIB_PATH):
     L = ctypes.CDLL(path)
     P = ctypes.POINTER(ProblemStruct)
     for f in ("kalman_gpu_smooth_oddeven_packed", "kalman_gpu_smooth_associative_packed",
-              "kalman_gpu_smooth_oddeven_noalloc"):
+              "kalman_gpu_smooth_oddeven_noalloc", "kalman_gpu_filter_packed"):
         getattr(L, f).argtypes = [ctypes.c_uint32, P, ctypes.c_void_p]
         getattr(L, f).restype = ctypes.c_int
     L.kalman_gpu_last_error.restype = ctypes.c_char_p
@@ -249,6 +250,17 @@ class DeviceProblem:
         opts = options_for(algorithm, covariance and self.cov is not None, fp32_refine, sweeps, tf32x3)
         f = L.kalman_gpu_smooth_oddeven_packed if algorithm == "oddeven" else L.kalman_gpu_smooth_associative_packed
         status = f(opts, ctypes.byref(self.struct), ctypes.c_void_p(st.cuda_stream))
+        if check:
+            _check(status)
+        return status
+
+    def filter(self, covariance=True, stream=None, check=True):
+        """Filtered estimates x_{s|s} (and P_{s|s}) of every step into
+        self.state / self.cov: kalman_gpu_filter_packed."""
+        L = load()
+        st = stream if stream is not None else self.torch.cuda.current_stream()
+        opts = 0 if (covariance and self.cov is not None) else KALMAN_NO_COVARIANCE
+        status = L.kalman_gpu_filter_packed(opts, ctypes.byref(self.struct), ctypes.c_void_p(st.cuda_stream))
         if check:
             _check(status)
         return status
