@@ -159,6 +159,268 @@ __global__ void __launch_bounds__(NT) filter_cta(FilterArgs a)
   }
 }
 
+/* ---------------------------------------------------------------------------
+ * Small states (n, mmax <= 8): one warp per track, lane j holding column j of
+ * the current panel in registers (fixed shapes, unused rows exactly zero, so
+ * no row counts reach register indices):
+ *   evolve panel  rows 0..N-1 the weighed [-F | H | c], rows N..2N-1 the
+ *                 carried [R | 0 | y] (zero rows past z), N pivots; rows
+ *                 N..2N-1 of columns N..2N are the information on x_i
+ *   observe panel rows 0..N-1 that information (shifted to lanes 0..N), rows
+ *                 N..N+7 the weighed [G | o] (zero past m), N pivots
+ * Reflectors are formed by the pivot column's lane and broadcast by shuffles.
+ * Weighing factors, R and R^{-1} for the estimate go through a small
+ * per-warp shared-memory area.
+ * ------------------------------------------------------------------------ */
+constexpr int kWarpsPerBlock = 4;
+constexpr int kWarpMaxN = 8;
+
+/* QR with NP pivots of the panel held as one column per lane (R rows, NC
+ * columns: lanes from NC on hold nothing and stay idle) */
+template <int R, int NP, int NC>
+__device__ __forceinline__ void warp_qr(double (&col)[R], int lane)
+{
+#pragma unroll
+  for (int k = 0; k < NP; ++k) {
+    double tail = 0.0;
+#pragma unroll
+    for (int i = k + 1; i < R; ++i) tail = fma(col[i], col[i], tail);
+    tail = __shfl_sync(0xffffffffu, tail, k);
+    const double alpha = __shfl_sync(0xffffffffu, col[k], k);
+    if (tail == 0.0) continue; /* identity reflector: uniform over the warp */
+    const double beta = -copysign(sqrt(fma(alpha, alpha, tail)), alpha);
+    const double amb = alpha - beta;
+    const double inv = 1.0 / (beta * amb);
+    const double t = -(amb * amb) * inv, scale = beta * inv;
+    double v[R];
+#pragma unroll
+    for (int i = k + 1; i < R; ++i) v[i] = __shfl_sync(0xffffffffu, col[i], k) * scale;
+    if (lane == k) {
+      col[k] = beta;
+#pragma unroll
+      for (int i = k + 1; i < R; ++i) col[i] = v[i];
+    } else if (lane > k && lane < NC) {
+      double d = col[k];
+#pragma unroll
+      for (int i = k + 1; i < R; ++i) d = fma(v[i], col[i], d);
+      d *= t;
+      col[k] -= d;
+#pragma unroll
+      for (int i = k + 1; i < R; ++i) col[i] = fma(-d, v[i], col[i]);
+    }
+  }
+}
+
+/* rows r0 .. r0+rows-1 of this lane's column <- V (those rows) for the factor
+ * of a covariance (column-major, ld ldc): 'W' W x, 'w' diag x, 'C'
+ * chol(cov)^{-1} x, 'U'/'F' tril(cov)^{-1} x.  sL: rows^2 doubles of the
+ * warp's shared area.  Returns false for a factor that is not positive
+ * definite or has a zero pivot (the same in every lane). */
+template <int R, int R0, int MAXR>
+__device__ __forceinline__ bool warp_weigh(double (&col)[R], char type, const double* cov, int ldc, int rows,
+                                           double* sL, int lane, int ncols)
+{
+  bool ok = true;
+  const bool act = lane < ncols; /* lanes past the panel's columns hold zeros */
+  if (type == 'w') {
+#pragma unroll
+    for (int i = 0; i < MAXR; ++i)
+      if (act && i < rows) col[R0 + i] *= cov[i];
+    return true;
+  }
+  if (type == 'W') {
+    if (!act) return true;
+    double x[MAXR];
+#pragma unroll
+    for (int i = 0; i < MAXR; ++i) {
+      double sm = 0.0;
+#pragma unroll
+      for (int k = 0; k < MAXR; ++k)
+        if (i < rows && k < rows) sm = fma(cov[(int64_t)k * ldc + i], col[R0 + k], sm);
+      x[i] = sm;
+    }
+#pragma unroll
+    for (int i = 0; i < MAXR; ++i)
+      if (i < rows) col[R0 + i] = x[i];
+    return true;
+  }
+  if (type != 'C' && type != 'U' && type != 'F') return true;
+  /* the factor, column-major rows x rows, lower triangle */
+  for (int e = lane; e < rows * rows; e += 32) {
+    const int j = e / rows, i = e - j * rows;
+    sL[e] = i >= j ? cov[(int64_t)j * ldc + i] : 0.0;
+  }
+  __syncwarp();
+  if (type == 'C') {
+    if (lane == 0) /* Cholesky by one lane: at most 8 x 8 */
+      for (int j = 0; j < rows; ++j) {
+        double d = sL[j * rows + j];
+        for (int k = 0; k < j; ++k) d = fma(-sL[k * rows + j], sL[k * rows + j], d);
+        const bool pd = d > 0.0;
+        const double ljj = pd ? sqrt(d) : 1.0;
+        sL[j * rows + j] = pd ? ljj : -1.0; /* -1 marks a failed pivot (sqrt >= 0 otherwise) */
+        for (int i = j + 1; i < rows; ++i) {
+          double x = sL[j * rows + i];
+          for (int k = 0; k < j; ++k) x = fma(-sL[k * rows + i], sL[k * rows + j], x);
+          sL[j * rows + i] = x / ljj;
+        }
+      }
+    __syncwarp();
+    for (int j = 0; j < rows; ++j)
+      if (sL[j * rows + j] < 0.0) {
+        ok = false;
+        sL[j * rows + j] = 1.0;
+      }
+    __syncwarp();
+  } else {
+    for (int j = 0; j < rows; ++j)
+      if (sL[j * rows + j] == 0.0) ok = false;
+  }
+  /* forward substitution on this lane's rows */
+#pragma unroll
+  for (int i = 0; i < MAXR; ++i)
+    if (act && i < rows) {
+      double x = col[R0 + i];
+#pragma unroll
+      for (int k = 0; k < MAXR; ++k)
+        if (k < i) x = fma(-sL[k * rows + i], col[R0 + k], x);
+      col[R0 + i] = x / sL[i * rows + i];
+    }
+  __syncwarp();
+  return ok;
+}
+
+template <int N>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) filter_warp(FilterArgs a)
+{
+  constexpr int RE = 2 * N, RO = N + kWarpMaxN;
+  __shared__ double area[kWarpsPerBlock][kWarpMaxN * kWarpMaxN + 2 * N * N + N];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int t = blockIdx.x * kWarpsPerBlock + w;
+  if (t >= a.ntracks) return; /* uniform over the warp */
+  double* sL = area[w];
+  double* sR = sL + kWarpMaxN * kWarpMaxN; /* R, column-major N x N */
+  double* sRi = sR + N * N;                 /* R^{-1}, column-major */
+  double* sy = sRi + N * N;
+  const int mm = a.mmax;
+  const int64_t nn = (int64_t)N * N;
+  const int64_t s0 = a.track_start[t], s1 = a.track_start[t + 1];
+  double Rc[N]; /* this lane's column of the carried [R | y] (lanes 0..N), zero rows past z */
+#pragma unroll
+  for (int r = 0; r < N; ++r) Rc[r] = 0.0;
+  int z = 0;
+  int flag = 0;
+  for (int64_t s = s0; s < s1; ++s) {
+    double oc[RO]; /* the observe panel: lanes 0..N-1 R~'s columns, lane N y~ */
+    if (s > s0) {
+      double ec[RE];
+      /* rows 0..N-1: [-F | H | c] of step s; rows N..2N-1: [R | 0 | y] */
+#pragma unroll
+      for (int r = 0; r < N; ++r) {
+        double v = 0.0;
+        if (lane < N) v = -a.F[s * nn + (int64_t)lane * N + r];
+        else if (lane < 2 * N) v = a.H[s * nn + (int64_t)(lane - N) * N + r];
+        else if (lane == 2 * N) v = a.c[s * N + r];
+        ec[r] = v;
+      }
+#pragma unroll
+      for (int r = 0; r < N; ++r) {
+        const double yr = __shfl_sync(0xffffffffu, Rc[r], N);
+        ec[N + r] = lane < N ? Rc[r] : lane == 2 * N ? yr : 0.0;
+      }
+      const char kt = a.K_type[s];
+      if (!cta::valid_cov_type(kt)) flag |= 4;
+      if (!warp_weigh<RE, 0, N>(ec, kt, a.K + s * nn, N, N, sL, lane, 2 * N + 1)) flag |= 1;
+      warp_qr<RE, N, 2 * N + 1>(ec, lane);
+      /* rows N..2N-1 of lanes N..2N -> lanes 0..N */
+#pragma unroll
+      for (int r = 0; r < N; ++r) oc[r] = __shfl_sync(0xffffffffu, ec[N + r], (lane + N) & 31);
+      if (lane > N) {
+#pragma unroll
+        for (int r = 0; r < N; ++r) oc[r] = 0.0;
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < N; ++r) oc[r] = 0.0;
+    }
+    int m = a.obs_rows[s];
+    if (m < 0 || m > mm || m > kWarpMaxN) {
+      flag |= 4;
+      m = 0;
+    }
+#pragma unroll
+    for (int r = 0; r < kWarpMaxN; ++r) {
+      double v = 0.0;
+      if (r < m) {
+        if (lane < N) v = a.G[s * (int64_t)mm * N + (int64_t)lane * mm + r];
+        else if (lane == N) v = a.o[s * mm + r];
+      }
+      oc[N + r] = v;
+    }
+    if (m > 0) {
+      const char ct = a.C_type[s];
+      if (!cta::valid_cov_type(ct)) flag |= 4;
+      if (!warp_weigh<RO, N, kWarpMaxN>(oc, ct, a.C + s * (int64_t)mm * mm, mm, m, sL, lane, N + 1)) flag |= 1;
+    }
+    warp_qr<RO, N, N + 1>(oc, lane);
+#pragma unroll
+    for (int r = 0; r < N; ++r) Rc[r] = (lane <= N && (lane == N || r <= lane)) ? oc[r] : 0.0;
+    z = z + m < N ? z + m : N;
+    /* estimate */
+    double* x = a.state + s * N;
+    double* P = a.cov ? a.cov + s * nn : nullptr;
+    bool det = z == N;
+    if (lane < N) {
+#pragma unroll
+      for (int r = 0; r < N; ++r) sR[lane * N + r] = Rc[r];
+    } else if (lane == N) {
+#pragma unroll
+      for (int r = 0; r < N; ++r) sy[r] = Rc[r];
+    }
+    __syncwarp();
+    for (int i = 0; i < N; ++i)
+      if (sR[i * N + i] == 0.0) det = false;
+    if (!det) {
+      if (lane < N) x[lane] = NAN;
+      if (P)
+        for (int e = lane; e < N * N; e += 32) P[e] = NAN;
+      flag |= 1;
+      __syncwarp();
+      continue;
+    }
+    if (lane < N) { /* column lane of R^{-1}: R u = e_lane */
+      double u[N];
+#pragma unroll
+      for (int i = N - 1; i >= 0; --i) {
+        double v = i == lane ? 1.0 : 0.0;
+#pragma unroll
+        for (int k = i + 1; k < N; ++k) v = fma(-sR[k * N + i], u[k], v);
+        u[i] = v / sR[i * N + i];
+      }
+#pragma unroll
+      for (int i = 0; i < N; ++i) sRi[lane * N + i] = u[i];
+    }
+    __syncwarp();
+    if (lane < N) {
+      double xi = 0.0;
+#pragma unroll
+      for (int k = 0; k < N; ++k) xi = fma(sRi[k * N + lane], sy[k], xi);
+      x[lane] = xi;
+      if (P) { /* P(:, lane) = sum_k Ri(:, k) Ri(lane, k) */
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          double sm = 0.0;
+#pragma unroll
+          for (int k = 0; k < N; ++k) sm = fma(sRi[k * N + i], sRi[k * N + lane], sm);
+          P[(int64_t)lane * N + i] = sm;
+        }
+      }
+    }
+    __syncwarp();
+  }
+  if (flag && lane == 0) atomicOr(a.flag, flag);
+}
+
 struct Workspace {
   void* p = nullptr;
   size_t bytes = 0;
@@ -231,7 +493,22 @@ extern "C" int kalman_gpu_filter_packed(uint32_t options, const kalman_gpu_probl
   a.scratch = (double*)(base + tab + 256);
   a.per_cta = per;
   a.flag = dflag;
-  UKG_LAUNCH(UKG_K_FILTER, st, (filter_cta<<<ncta, NT, 0, st>>>(a)));
+  if (p->n <= kWarpMaxN && p->mmax <= kWarpMaxN) {
+    const unsigned blocks = (unsigned)((p->ntracks + kWarpsPerBlock - 1) / kWarpsPerBlock);
+    const int bs = 32 * kWarpsPerBlock;
+    switch (p->n) {
+      case 1: UKG_LAUNCH(UKG_K_FILTER, st, (filter_warp<1><<<blocks, bs, 0, st>>>(a))); break;
+      case 2: UKG_LAUNCH(UKG_K_FILTER, st, (filter_warp<2><<<blocks, bs, 0, st>>>(a))); break;
+      case 3: UKG_LAUNCH(UKG_K_FILTER, st, (filter_warp<3><<<blocks, bs, 0, st>>>(a))); break;
+      case 4: UKG_LAUNCH(UKG_K_FILTER, st, (filter_warp<4><<<blocks, bs, 0, st>>>(a))); break;
+      case 5: UKG_LAUNCH(UKG_K_FILTER, st, (filter_warp<5><<<blocks, bs, 0, st>>>(a))); break;
+      case 6: UKG_LAUNCH(UKG_K_FILTER, st, (filter_warp<6><<<blocks, bs, 0, st>>>(a))); break;
+      case 7: UKG_LAUNCH(UKG_K_FILTER, st, (filter_warp<7><<<blocks, bs, 0, st>>>(a))); break;
+      default: UKG_LAUNCH(UKG_K_FILTER, st, (filter_warp<8><<<blocks, bs, 0, st>>>(a))); break;
+    }
+  } else {
+    UKG_LAUNCH(UKG_K_FILTER, st, (filter_cta<<<ncta, NT, 0, st>>>(a)));
+  }
   int hflag = 0;
   cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaError_t e = cudaStreamSynchronize(st);
