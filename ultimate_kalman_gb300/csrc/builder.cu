@@ -24,18 +24,32 @@ __global__ void expand_matrix(double* __restrict__ dst, int64_t first, int64_t k
                               const double* __restrict__ s0, int r0, int c0, const double* __restrict__ s1, int r1,
                               int c1)
 {
-  const int64_t per = (int64_t)rows * cols, total = k * per;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = e / per;
-    const int64_t w = e - i * per;
-    const int j = (int)(w / rows), r = (int)(w - (int64_t)j * rows);
+  const int per = rows * cols; /* <= 128 x 128 */
+  const int64_t total = k * per, e0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e0 >= total) return;
+  /* (step, entry) of this thread's entries, advanced by the grid stride without
+     64-bit divisions in the loop */
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t sq = stride / per;
+  const int sr = (int)(stride - sq * per);
+  int64_t i = e0 / per;
+  int w = (int)(e0 - i * per);
+  double* out = dst + first * per;
+  for (int64_t e = e0; e < total; e += stride) {
+    const int j = w / rows, r = w - j * rows;
     double v = 0.0;
     if (i == 0) {
       if (s0 && r < r0 && j < c0) v = s0[(int64_t)j * r0 + r];
     } else if (s1 && r < r1 && j < c1) {
       v = s1[(int64_t)j * r1 + r];
     }
-    dst[(first + i) * per + w] = v;
+    out[e] = v;
+    i += sq;
+    w += sr;
+    if (w >= per) {
+      w -= per;
+      ++i;
+    }
   }
 }
 
