@@ -51,7 +51,8 @@ def synthetic_track(k, n, m, rho=0.99, lo=0.1, hi=1.0, log_cov=False, missing=0.
     return P
 
 
-def device_track(k, n, m, rho=0.99, lo=0.1, hi=1.0, log_cov=False, missing=0.05, seed=0, covariance=True):
+def device_track(k, n, m, rho=0.99, lo=0.1, hi=1.0, log_cov=False, missing=0.05, seed=0, covariance=True,
+                 with_builder=False):
     """synthetic_track's track built on the GPU by the library's equation
     builder (kalman_gpu_expand_invariant): only the model, the observations
     and the step row counts cross the host link, so tracks of 10^6 steps with
@@ -84,10 +85,13 @@ def device_track(k, n, m, rho=0.99, lo=0.1, hi=1.0, log_cov=False, missing=0.05,
                                K=keep[3].data_ptr(), K_type=b"C", G0=eye.data_ptr(), o0=keep[4].data_ptr(),
                                C0=eye.data_ptr(), C0_type=b"C", G=keep[5].data_ptr(), C=keep[6].data_ptr(),
                                C_type=b"C")
-    native.expand_invariant(D.struct, 0, k, md, keep[7].data_ptr(), m, keep[8].data_ptr(),
-                            torch.cuda.current_stream())
+    def build():
+        native.expand_invariant(D.struct, 0, k, md, keep[7].data_ptr(), m, keep[8].data_ptr(),
+                                torch.cuda.current_stream())
+
+    build()
     torch.cuda.synchronize()
-    return D
+    return (D, build) if with_builder else D
 
 
 def main():
@@ -106,7 +110,24 @@ def main():
     ap.add_argument("--log-cov", action="store_true", help="covariance eigenvalues log-uniform in [1e-3, 1]")
     ap.add_argument("--device-build", action="store_true",
                     help="build the track on the GPU with the equation builder (no host copy of the equations)")
+    ap.add_argument("--time-build", action="store_true",
+                    help="time the equation builder on the track (CUDA events) instead of smoothing it")
     args = ap.parse_args()
+    if args.time_build:
+        D, build = device_track(args.k, args.n, args.m, covariance=False, with_builder=True)
+        for _ in range(3):
+            build()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(args.repeats):
+            build()
+        e.record()
+        torch.cuda.synchronize()
+        ms = s.elapsed_time(e) / args.repeats
+        written = D.input_bytes()
+        print(json.dumps({"n": args.n, "m": args.m, "k": args.k, "build_ms": ms, "written_gb": written / 1e9,
+                          "write_gbs": written / (ms * 1e-3) / 1e9}))
+        return
     lo = 1e-3 if args.log_cov else 0.1
     rho = 0.995 if args.n >= 128 else 0.99
     cov = not args.no_covariance and not args.fp32_refine
