@@ -218,7 +218,7 @@ __device__ __forceinline__ void warp_qr(double (&col)[R], int lane)
  * definite or has a zero pivot (the same in every lane). */
 template <int R, int R0, int MAXR>
 __device__ __forceinline__ bool warp_weigh(double (&col)[R], char type, const double* cov, int ldc, int rows,
-                                           double* sL, int lane, int ncols)
+                                           double* sL, double* sInv, int lane, int ncols)
 {
   bool ok = true;
   const bool act = lane < ncols; /* lanes past the panel's columns hold zeros */
@@ -252,27 +252,27 @@ __device__ __forceinline__ bool warp_weigh(double (&col)[R], char type, const do
   }
   __syncwarp();
   if (type == 'C') {
-    if (lane == 0) /* Cholesky by one lane: at most 8 x 8 */
+    if (lane == 0) /* Cholesky by one lane: at most 8 x 8; one division per column */
       for (int j = 0; j < rows; ++j) {
         double d = sL[j * rows + j];
         for (int k = 0; k < j; ++k) d = fma(-sL[k * rows + j], sL[k * rows + j], d);
         const bool pd = d > 0.0;
         const double ljj = pd ? sqrt(d) : 1.0;
+        const double ri = 1.0 / ljj;
         sL[j * rows + j] = pd ? ljj : -1.0; /* -1 marks a failed pivot (sqrt >= 0 otherwise) */
+        sInv[j] = ri;
         for (int i = j + 1; i < rows; ++i) {
           double x = sL[j * rows + i];
           for (int k = 0; k < j; ++k) x = fma(-sL[k * rows + i], sL[k * rows + j], x);
-          sL[j * rows + i] = x / ljj;
+          sL[j * rows + i] = x * ri;
         }
       }
     __syncwarp();
     for (int j = 0; j < rows; ++j)
-      if (sL[j * rows + j] < 0.0) {
-        ok = false;
-        sL[j * rows + j] = 1.0;
-      }
-    __syncwarp();
+      if (sL[j * rows + j] < 0.0) ok = false;
   } else {
+    if (lane < rows) sInv[lane] = 1.0 / sL[lane * rows + lane];
+    __syncwarp();
     for (int j = 0; j < rows; ++j)
       if (sL[j * rows + j] == 0.0) ok = false;
   }
@@ -284,7 +284,7 @@ __device__ __forceinline__ bool warp_weigh(double (&col)[R], char type, const do
 #pragma unroll
       for (int k = 0; k < MAXR; ++k)
         if (k < i) x = fma(-sL[k * rows + i], col[R0 + k], x);
-      col[R0 + i] = x / sL[i * rows + i];
+      col[R0 + i] = x * sInv[i];
     }
   __syncwarp();
   return ok;
@@ -294,7 +294,7 @@ template <int N>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) filter_warp(FilterArgs a)
 {
   constexpr int RE = 2 * N, RO = N + kWarpMaxN;
-  __shared__ double area[kWarpsPerBlock][kWarpMaxN * kWarpMaxN + 2 * N * N + N];
+  __shared__ double area[kWarpsPerBlock][kWarpMaxN * kWarpMaxN + 2 * N * N + N + kWarpMaxN + N];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int t = blockIdx.x * kWarpsPerBlock + w;
   if (t >= a.ntracks) return; /* uniform over the warp */
@@ -302,6 +302,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) filter_warp(FilterArgs a)
   double* sR = sL + kWarpMaxN * kWarpMaxN; /* R, column-major N x N */
   double* sRi = sR + N * N;                 /* R^{-1}, column-major */
   double* sy = sRi + N * N;
+  double* sInv = sy + N;          /* reciprocal pivots of the weighing factor */
+  double* sInvR = sInv + kWarpMaxN; /* reciprocal diagonal of R */
   const int mm = a.mmax;
   const int64_t nn = (int64_t)N * N;
   const int64_t s0 = a.track_start[t], s1 = a.track_start[t + 1];
@@ -330,7 +332,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) filter_warp(FilterArgs a)
       }
       const char kt = a.K_type[s];
       if (!cta::valid_cov_type(kt)) flag |= 4;
-      if (!warp_weigh<RE, 0, N>(ec, kt, a.K + s * nn, N, N, sL, lane, 2 * N + 1)) flag |= 1;
+      if (!warp_weigh<RE, 0, N>(ec, kt, a.K + s * nn, N, N, sL, sInv, lane, 2 * N + 1)) flag |= 1;
       warp_qr<RE, N, 2 * N + 1>(ec, lane);
       /* rows N..2N-1 of lanes N..2N -> lanes 0..N */
 #pragma unroll
@@ -360,7 +362,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) filter_warp(FilterArgs a)
     if (m > 0) {
       const char ct = a.C_type[s];
       if (!cta::valid_cov_type(ct)) flag |= 4;
-      if (!warp_weigh<RO, N, kWarpMaxN>(oc, ct, a.C + s * (int64_t)mm * mm, mm, m, sL, lane, N + 1)) flag |= 1;
+      if (!warp_weigh<RO, N, kWarpMaxN>(oc, ct, a.C + s * (int64_t)mm * mm, mm, m, sL, sInv, lane, N + 1)) flag |= 1;
     }
     warp_qr<RO, N, N + 1>(oc, lane);
 #pragma unroll
@@ -388,6 +390,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) filter_warp(FilterArgs a)
       __syncwarp();
       continue;
     }
+    if (lane < N) sInvR[lane] = 1.0 / sR[lane * N + lane];
+    __syncwarp();
     if (lane < N) { /* column lane of R^{-1}: R u = e_lane */
       double u[N];
 #pragma unroll
@@ -395,7 +399,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) filter_warp(FilterArgs a)
         double v = i == lane ? 1.0 : 0.0;
 #pragma unroll
         for (int k = i + 1; k < N; ++k) v = fma(-sR[k * N + i], u[k], v);
-        u[i] = v / sR[i * N + i];
+        u[i] = v * sInvR[i];
       }
 #pragma unroll
       for (int i = 0; i < N; ++i) sRi[lane * N + i] = u[i];
