@@ -153,3 +153,37 @@ def test_matrix_helpers_match_numpy(lib):
     W = np.linalg.inv(np.linalg.cholesky(C))
     Ce = native._read_matrix(L.kalman_covariance_matrix_explicit(_mat(L, W, keep), b"W"))
     np.testing.assert_allclose(Ce, C, rtol=1e-9)
+
+
+def test_builder_and_filter_refuse_bad_arguments_without_touching_a_device(lib):
+    """kalman_gpu_expand_invariant and kalman_gpu_filter_packed check their
+    arguments on the host first: host-array problems, step ranges outside the
+    problem, observation rows above mmax and unknown covariance types are
+    refused with EINVAL before any CUDA call."""
+    from ultimate_kalman_gb300 import problem
+    P = problem.constant_velocity([5], seed=1)
+    keep = []
+    s = native.ProblemStruct()
+    s.n, s.mmax, s.ntracks, s.location, s.nsteps = P.n, P.mmax, 1, native.KALMAN_GPU_HOST, P.nsteps
+    ts = np.ascontiguousarray(P.track_start, dtype=np.int64)
+    s.track_start = ts.ctypes.data
+    arrs = {f: np.ascontiguousarray(getattr(P, f)) for f in native._FIELDS}
+    for f, a in arrs.items():
+        setattr(s, f, a.ctypes.data)
+    state = np.zeros((P.nsteps, P.n))
+    s.state = state.ctypes.data
+    assert lib.kalman_gpu_filter_packed(native.KALMAN_NO_COVARIANCE, ctypes.byref(s), None) == native.KALMAN_GPU_EINVAL
+    assert "device arrays" in native.last_error()[1]
+    md = native.InvariantModel(m0=P.n, m=3, K_type=b"C", C0_type=b"W", C_type=b"C")
+    assert lib.kalman_gpu_expand_invariant(ctypes.byref(s), 0, 5, ctypes.byref(md), None, 3, None, None) == \
+        native.KALMAN_GPU_EINVAL  # host arrays
+    s.location = native.KALMAN_GPU_DEVICE
+    assert lib.kalman_gpu_expand_invariant(ctypes.byref(s), 3, 5, ctypes.byref(md), None, 3, None, None) == \
+        native.KALMAN_GPU_EINVAL  # steps 3..7 of a 5-step problem
+    bad = native.InvariantModel(m0=P.mmax + 1, m=3, K_type=b"C", C0_type=b"W", C_type=b"C")
+    assert lib.kalman_gpu_expand_invariant(ctypes.byref(s), 0, 5, ctypes.byref(bad), None, 3, None, None) == \
+        native.KALMAN_GPU_EINVAL
+    bad = native.InvariantModel(m0=P.n, m=3, K_type=b"Q", C0_type=b"W", C_type=b"C")
+    assert lib.kalman_gpu_expand_invariant(ctypes.byref(s), 0, 5, ctypes.byref(bad), None, 3, None, None) == \
+        native.KALMAN_GPU_EINVAL
+    assert "covariance types" in native.last_error()[1]
