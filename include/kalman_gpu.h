@@ -112,7 +112,7 @@ int kalman_gpu_smooth_tracks(uint32_t options, kalman_step_equations_t** equatio
                              const kalman_step_index_t* track_lengths, int32_t ntracks);
 
 /* Filtered estimates (the sequential UltimateKalman filter of
- * c/kalman_ultimate.c: evolve 140-330, observe 332-470, estimate 472-557) for
+ * c/kalman_ultimate.c: evolve 140-345, observe 347-557 with its estimate 508-545) for
  * every step of every track of a packed problem with DEVICE arrays: state[s]
  * = x_{s|s} and, unless KALMAN_NO_COVARIANCE, covariance[s] = P_{s|s}
  * (column-major), from the equations of the track's steps up to s.  Steps

@@ -1,8 +1,10 @@
 /*
  * filter.cu -- filtered estimates on the device: the sequential UltimateKalman
- * filter (c/kalman_ultimate.c: evolve 140-330, observe 332-470, estimate
- * 472-557) run for every track of a packed problem at once, one thread block
- * per track (kalman_gpu_filter_packed).
+ * filter (c/kalman_ultimate.c: evolve 140-345, observe 347-557 with its
+ * estimate 508-545) run for every track of a packed problem at once, one
+ * thread block per track (kalman_gpu_filter_packed).  The reference keeps the
+ * covariance as the factor R (its covariance_type 'W'); here P = R^{-1} R^{-T}
+ * is written explicitly, as the smoothers write theirs.
  *
  * Per track the block keeps the factor of the current state's information,
  * an upper-trapezoidal R (z rows, z <= n) and its right-hand side y:
