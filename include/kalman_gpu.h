@@ -177,7 +177,11 @@ double  kalman_gpu_measure_fp32_tflops(void);
  * caller passes the input and output arrays.  The first call on a device looks
  * up the array's device address (make it before any stream capture).  Calls
  * share the array: they are serialized and each waits for its kernels; work
- * that overlapped a call on the GPU would race on it.                        */
+ * that overlapped a call on the GPU would race on it.  Every call blocks the
+ * host until its kernels have finished: it synchronizes the stream to read the
+ * status.  It runs the plain FP64 smoother (per-thread kernels at every state
+ * dimension up to the scratch limit); KALMAN_GPU_FP32_REFINE and
+ * KALMAN_GPU_TF32X3 are refused with KALMAN_GPU_EINVAL.                      */
 #define KALMAN_GPU_NOALLOC_SCRATCH_BYTES (64u << 20)
 int kalman_gpu_smooth_oddeven_noalloc(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream);
 
@@ -203,6 +207,16 @@ kalman_gpu_plan_t* kalman_gpu_plan_create(uint32_t options, const kalman_gpu_pro
 int kalman_gpu_plan_execute(kalman_gpu_plan_t* plan, void* cuda_stream);
 int kalman_gpu_plan_status(kalman_gpu_plan_t* plan);
 void kalman_gpu_plan_destroy(kalman_gpu_plan_t* plan);
+
+/* HBM accounting for callers that budget device memory (a serving loop
+ * admitting requests by memory; no reference counterpart).
+ * kalman_gpu_oddeven_workspace_bytes: device bytes kalman_gpu_smooth_oddeven_packed
+ * caches for problem p under these options (its workspace grows to the
+ * largest problem a host thread has smoothed and is kept); -1 if p is
+ * malformed.  kalman_gpu_workspace_held: device bytes of workspace and
+ * staging the calling host thread holds now (all entry points).            */
+int64_t kalman_gpu_oddeven_workspace_bytes(uint32_t options, const kalman_gpu_problem_t* p);
+int64_t kalman_gpu_workspace_held(void);
 
 /* Releases the device workspace and pinned staging buffers cached by the
  * library for the current device.                                            */

@@ -24,7 +24,8 @@ import subprocess
 import sys
 import tempfile
 
-REF_C = "/root/reference/c"
+# the reference C sources: UKG_REFERENCE_C, else where the build machine keeps them
+REF_C = os.environ.get("UKG_REFERENCE_C", "/root/reference/c")
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_ref")
 OUT_LIB = os.path.join(OUT_DIR, "libukref.so")

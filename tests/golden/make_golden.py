@@ -38,7 +38,8 @@ sys.path.insert(0, REPO)
 from ultimate_kalman_gb300 import problem as pb  # noqa: E402
 
 REF_LIB = os.path.join(REPO, "oracle", "_ref", "libukref.so")
-REF_C = "/root/reference/c"
+# the reference C sources: UKG_REFERENCE_C, else where the build machine keeps them
+REF_C = os.environ.get("UKG_REFERENCE_C", "/root/reference/c")
 
 ALG = {"ultimate": 1, "oddeven": 4, "associative": 8}
 

@@ -15,6 +15,7 @@ import ctypes
 import numpy as np
 import pytest
 
+import oracle
 from ultimate_kalman_gb300 import native, problem as pb
 
 pytestmark = pytest.mark.gpu
@@ -29,7 +30,7 @@ def lib():
     return native.load()
 
 
-def run_noalloc(L, D, covariance=True):
+def run_noalloc(L, D, covariance=True, opts=None):
     """Calls the allocation-free entry point on the device arrays of D, writing
     into freshly allocated output buffers of the caller."""
     import torch
@@ -38,7 +39,8 @@ def run_noalloc(L, D, covariance=True):
     s = native.ProblemStruct.from_buffer_copy(D.struct)
     s.state = state.data_ptr()
     s.covariance = cov.data_ptr() if covariance else None
-    opts = native.options_for("oddeven", covariance)
+    if opts is None:
+        opts = native.options_for("oddeven", covariance)
     st = torch.cuda.current_stream()
     status = L.kalman_gpu_smooth_oddeven_noalloc(opts, ctypes.byref(s), ctypes.c_void_p(st.cuda_stream))
     X = state.cpu().numpy()
@@ -66,6 +68,36 @@ def test_matches_ordinary_entry_point_on_consecutive_calls(lib):
         status, X2, _ = run_noalloc(lib, D, covariance=False)
         assert status == 0
         assert rel(X2, Xr) < TOL
+
+
+# Shapes at which the ordinary entry point runs CTA kernels (n >= 9 or more
+# than 8 observation rows) while this entry point keeps the per-thread ones.
+LARGE_SHAPES = [(12, 6, [900, 77, 2]), (24, 12, [300, 41]), (6, 12, [800, 65])]
+
+
+@pytest.mark.parametrize("n,m,lengths", LARGE_SHAPES, ids=[f"n{n}_m{m}" for n, m, _ in LARGE_SHAPES])
+def test_larger_shapes_match_ordinary_entry_point_and_oracle(lib, n, m, lengths):
+    P = pb.random_dynamics(lengths, n, m, seed=n + m, per_step=False, missing=0.1)
+    D = native.DeviceProblem(P, covariance=True)
+    D.smooth("oddeven", covariance=True)
+    Xr, Sr = D.results()
+    st, Xo, So = oracle.smooth(P, "oddeven")
+    assert st == 0
+    for call in range(2):  # the second call finds the first one's contents in the array
+        status, X, S = run_noalloc(lib, D)
+        assert status == 0, native.last_error()
+        assert rel(X, Xr) < TOL and rel(S, Sr) < TOL, (call, rel(X, Xr), rel(S, Sr))
+        assert rel(X, Xo) < TOL and rel(S, So) < TOL, (call, rel(X, Xo), rel(S, So))
+
+
+def test_refuses_the_precision_form(lib):
+    P = pb.constant_velocity([50], seed=6)
+    D = native.DeviceProblem(P, covariance=False)
+    for extra in (native.KALMAN_GPU_FP32_REFINE, native.KALMAN_GPU_FP32_REFINE | native.KALMAN_GPU_TF32X3):
+        opts = native.options_for("oddeven", False) | extra
+        status, X, _ = run_noalloc(lib, D, covariance=False, opts=opts)
+        assert status == 1
+        assert "plain FP64" in native.last_error()[1]
 
 
 def test_refuses_problems_beyond_the_scratch_array(lib):

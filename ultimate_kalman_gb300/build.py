@@ -7,6 +7,7 @@ them into ultimate_kalman_gb300/libukgpu.so.  Run directly or through
 from __future__ import annotations
 
 import concurrent.futures as cf
+import glob
 import os
 import shutil
 import subprocess
@@ -48,8 +49,9 @@ def _compile(src, verbose):
 
 def build(verbose=False, force=False):
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
-    deps = srcs + [os.path.join(CSRC, "ukgpu_internal.h"), os.path.join(CSRC, "profiling.h")] + [os.path.join(REPO, "include", h) for h in
-                                                              ("kalman.h", "kalman_gpu.h", "matrix_ops.h")]
+    # every header of the library and of include/ is a dependency of every object
+    deps = srcs + sorted(glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
+                         glob.glob(os.path.join(REPO, "include", "*.h")))
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in deps):
         return LIB
     os.makedirs(BUILD, exist_ok=True)

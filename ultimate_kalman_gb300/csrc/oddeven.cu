@@ -2847,6 +2847,8 @@ int ensure_workspace(size_t bytes, void** out)
 
 }  // namespace
 
+extern "C" int64_t ukg_oddeven_workspace_held(void) { return (int64_t)tl_ws.dev_bytes; }
+
 extern "C" void ukg_release_oddeven_workspace(void)
 {
   if (tl_ws.dev) cudaFree(tl_ws.dev);
@@ -3140,6 +3142,29 @@ extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* 
   return run_plan<double>(options, p, (cudaStream_t)cuda_stream, P, tab, (char*)base, tl_mtab.dev);
 }
 
+/* Device bytes the ordinary odd-even entry point caches for problem p under
+ * these options (the workspace of ukg_oddeven_device, with its 1/8 slack):
+ * a caller that budgets HBM (the serving loop) reads the library's own
+ * figure instead of modelling it.  -1 on a malformed problem.              */
+extern "C" int64_t kalman_gpu_oddeven_workspace_bytes(uint32_t options, const kalman_gpu_problem_t* p)
+{
+  ukg_clear_error();
+  if (ukg_validate_problem(p, 0)) return -1;
+  if (p->nsteps == 0) return 0;
+  const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
+  const bool f32 = (options & KALMAN_GPU_FP32_REFINE) != 0;
+  const int mxp = p->mmax > p->n ? p->mmax : p->n;
+  Plan P;
+  if (build_plan(p, want_cov, f32, f32, P, nullptr, 0) == 0) {
+    ukg_set_error(KALMAN_GPU_EINVAL, "tracks longer than 2^%d steps", kMaxLevels - 1);
+    return -1;
+  }
+  size_t bytes = P.bytes;
+  if (p->n >= kCtaMinN || mxp > 8)
+    bytes = align_up(P.bytes, 256) + (size_t)cta_count() * cta_scratch_per_cta(p->n, p->mmax) * sizeof(double);
+  return (int64_t)(bytes + (bytes >> 3));
+}
+
 /* ---------------------------------------------------------------------------
  * Allocation-free entry point (kalman_gpu_smooth_oddeven_noalloc).
  *
@@ -3181,6 +3206,9 @@ extern "C" int kalman_gpu_smooth_oddeven_noalloc(uint32_t options, const kalman_
   if (p->location != KALMAN_GPU_DEVICE)
     return ukg_set_error(KALMAN_GPU_EINVAL, "the allocation-free entry point takes device arrays only "
                          "(host arrays would need a device copy)");
+  if (options & (KALMAN_GPU_FP32_REFINE | KALMAN_GPU_TF32X3))
+    return ukg_set_error(KALMAN_GPU_EINVAL, "the allocation-free entry point runs the plain FP64 smoother only "
+                         "(KALMAN_GPU_FP32_REFINE and KALMAN_GPU_TF32X3 are not accepted)");
   if (p->nsteps == 0) return 0;
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
   int dev = 0;
@@ -3212,8 +3240,11 @@ extern "C" int kalman_gpu_smooth_oddeven_noalloc(uint32_t options, const kalman_
                          "point has %zu (use kalman_gpu_smooth_oddeven_packed)", P.bytes,
                          (size_t)KALMAN_GPU_NOALLOC_SCRATCH_BYTES);
   const int prof = ukg_prof_pause(); /* profiling would create CUDA events */
-  const int status = run_plan<double>(options & ~(uint32_t)KALMAN_GPU_FP32_REFINE, p, (cudaStream_t)cuda_stream, P,
-                                      g_noalloc_tab, (char*)g_noalloc_addr[dev]);
+  /* the per-thread kernels at every shape, also n >= 9 or mmax > 8 where the
+     ordinary entry point switches to CTA kernels (their per-CTA panels are
+     not part of this fixed scratch) */
+  const int status = run_plan<double>(options, p, (cudaStream_t)cuda_stream, P, g_noalloc_tab,
+                                      (char*)g_noalloc_addr[dev]);
   ukg_prof_resume(prof);
   return status;
 }
