@@ -188,11 +188,15 @@ def time_smooths(D, steps, stream, **kw):
     return evs[0].elapsed_time(evs[-1]) / steps, per
 
 
-def roofline_for(prof, fl, steps, fp64_peak, fp32_peak, hbm_peak, bytes_model):
-    """Roofline of the kernel category with the largest time.  FP64 kernels
-    are placed against the FP64 pipe or HBM, whichever fraction is higher;
-    the precision form's kernels (FP32 and double-float arithmetic on the FP32
-    pipe, far below its peak) against HBM."""
+def roofline_for(prof, fl, steps, fp64_peak, fp32_peak, hbm_peak, compulsory_in, traffic_model):
+    """Roofline of the kernel category with the largest time.
+
+    Algorithmic bytes are the problem's compulsory bytes (every step's
+    equations read once at their real sizes, flops.compulsory_bytes): they are
+    credited to the kernel that reads the caller's equations (the weighing
+    kernel); the other kernels move only intermediates, whose modelled bytes
+    are reported as traffic, not as algorithmic work.  FP64 kernels are placed
+    against the FP64 pipe when their flop fraction is the higher one."""
     top = max(prof, key=lambda k: prof[k][0])
     kms, kl = prof[top]
     secs = kms * 1e-3 / steps
@@ -200,17 +204,54 @@ def roofline_for(prof, fl, steps, fp64_peak, fp32_peak, hbm_peak, bytes_model):
     is32 = top.startswith("fp32") or top.startswith("refine") or top not in fl
     peak_f = fp32_peak if is32 else fp64_peak
     ach_f = flops / secs / 1e12
-    ach_b = bytes_model.get(top, 0.0) / secs / 1e9
+    alg = compulsory_in if top == "weigh_kernel" else 0.0
+    ach_b = alg / secs / 1e9
     frac_f, frac_b = ach_f / peak_f, ach_b / hbm_peak
-    if frac_b > frac_f or is32:
+    if frac_b >= frac_f:
         r = {"bound": "hbm", "achieved": ach_b, "peak": hbm_peak, "unit": "GB/s", "frac": frac_b,
-             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+             "algorithmic_bytes_per_launch": alg / max(1.0, kl / steps)}
     else:
         r = {"bound": "fp32" if is32 else "fp64", "achieved": ach_f, "peak": peak_f, "unit": "TFLOP/s",
              "frac": frac_f, "peak_source": "FMA-chain probe kernel timed in this run (of measured)"}
-    r.update({"kernel": top, "traffic": None, "fp_tflops": ach_f, "fp_frac": frac_f, "hbm_gbs": ach_b,
-              "hbm_frac": frac_b, "flops_model": "ultimate_kalman_gb300/flops.py (FMA = 2 flops)"})
+    r.update({"kernel": top, "traffic": None, "ms_per_step": kms / steps, "launches_per_step": kl / steps,
+              "fp_tflops": ach_f, "fp_frac": frac_f, "modelled_traffic_bytes": traffic_model.get(top),
+              "flops_model": "ultimate_kalman_gb300/flops.py (FMA = 2 flops)",
+              "bytes_model": "flops.compulsory_bytes: F, H, K, c, G, o, C at real sizes in; states out"})
     return r
+
+
+def whole_step(compulsory, ms, hbm_peak):
+    """The whole smoothing against HBM: compulsory bytes in + out over the
+    time of one smoothing."""
+    b = compulsory[0] + compulsory[1]
+    gbs = b / (ms * 1e-3) / 1e9
+    return {"algorithmic_bytes": b, "ms": ms, "achieved_gbs": gbs, "frac": gbs / hbm_peak,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+
+
+def rel_states(X, Xref):
+    """max over steps of ||x - xref||_inf / ||xref||_inf (torch or numpy)."""
+    if hasattr(X, "abs"):
+        num = (X - Xref).abs().reshape(len(X), -1).amax(dim=1)
+        den = Xref.abs().reshape(len(X), -1).amax(dim=1)
+        return float((num / den).max().item())
+    num = np.abs(X - Xref).reshape(len(X), -1).max(axis=1)
+    den = np.abs(Xref).reshape(len(X), -1).max(axis=1)
+    return float((num / den).max())
+
+
+def time_call(fn, reps, stream):
+    """Mean ms of `reps` calls of fn() bracketed by CUDA events on `stream`."""
+    import torch
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    s.record(stream)
+    for _ in range(reps):
+        fn()
+    e.record(stream)
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / reps
 
 
 def run_gpu(args):
@@ -280,13 +321,15 @@ def run_gpu(args):
     fl64 = flops.plan_flops_fast(P.track_lengths(), 6, 3, covariance=True)
     by32 = flops.plan_bytes_fast(P.track_lengths(), 6, 3, fp32=True, sweeps=args.sweeps or 2)
     by64 = flops.plan_bytes_fast(P.track_lengths(), 6, 3, fp32=False)
-    roof = roofline_for(prof, fl32, args.steps, peak64, peak32, peaks["hbm_gbs"], by32)
+    comp = flops.compulsory_bytes(P.track_lengths(), 6, 3, covariance=False)
+    comp_cov = flops.compulsory_bytes(P.track_lengths(), 6, 3, covariance=True)
+    roof = roofline_for(prof, fl32, args.steps, peak64, peak32, peaks["hbm_gbs"], comp[0], by32)
     tfile = os.path.join(REPO, "profiles", "traffic_per_launch.json")
     if os.path.exists(tfile):
         roof["traffic"] = json.load(open(tfile)).get(roof["kernel"])
     roof["per_kernel"] = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps,
                               "share": v[0] / sum(x[0] for x in prof.values())} for k, v in prof.items()}
-    roof64 = roofline_for(prof64, fl64, max(2, args.steps // 2), peak64, peak32, peaks["hbm_gbs"], by64)
+    roof64 = roofline_for(prof64, fl64, max(2, args.steps // 2), peak64, peak32, peaks["hbm_gbs"], comp_cov[0], by64)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -294,7 +337,8 @@ def run_gpu(args):
             "config": config_dict(P, args.tracks, world), "gpu_launches": int(launches),
             "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
                            "what": "one smoothing of all 4,096 tracks"},
-            "rel_err_vs_fp64": err, "roofline": roof, "clocks": clocks,
+            "rel_err_vs_fp64": err, "roofline": roof, "whole_step": whole_step(comp, ms, peaks["hbm_gbs"]),
+            "clocks": clocks,
             "plain_fp64": {"states_and_covariances": total_steps / (ms64c * 1e-3),
                            "states_only": total_steps / (ms64 * 1e-3), "unit": UNIT,
                            "speedup_fp32_refine_vs_fp64_states_only": ms64 / ms,
@@ -321,9 +365,12 @@ def run_gpu(args):
             times.append(time.perf_counter() - t0)
         e2e_ms = 1e3 * float(np.median(times))
         h2d = sum(t.numel() * t.element_size() for t in pin.values())
+        link = h2d_probe()
         line["e2e"] = {"value": total_steps / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                        "d2h_bytes_per_step": int(st_h.numel() * 8), "ms_per_step": e2e_ms,
-                       "path": "kalman_gpu_smooth_oddeven_packed, KALMAN_GPU_HOST arrays, FP32 + refinement"}
+                       "path": "kalman_gpu_smooth_oddeven_packed, KALMAN_GPU_HOST arrays, FP32 + refinement",
+                       "host_link": link, "h2d_share_at_probe_bandwidth": h2d / (link["h2d_gbs"] * 1e9) / (e2e_ms * 1e-3),
+                       "all_times_ms": [1e3 * t for t in times]}
 
     if rank == 0 and world == 1 and not args.no_cpu:
         v, nsteps, ntr, nt, dt, Xo = cpu_sample(P, args.cpu_seconds)
@@ -337,8 +384,11 @@ def run_gpu(args):
         if not args.no_e2e:
             del pin, st_h, s
         torch.cuda.empty_cache()
-        line["large_state"] = large_state(stream)
-        line["builder"] = builder_line()
+        for key, fn in (("large_state", lambda: large_state(stream)), ("builder", builder_line),
+                        ("config0", lambda: config0_line(stream, not args.no_cpu)),
+                        ("config1", lambda: config1_line(stream, not args.no_cpu)), ("serving", serving_line)):
+            native.release()
+            line[key] = secondary(fn)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -415,6 +465,183 @@ def large_state(stream):
            "speedup_fp32_refine_vs_fp64": ms64 / ms32}
     del D
     torch.cuda.empty_cache()
+    return out
+
+
+def secondary(fn):
+    """Runs one secondary leg of the bench; a failure is reported in its key
+    (with the library's message) instead of ending the run."""
+    import torch
+    try:
+        return fn()
+    except Exception as e:  # the headline line must still be printed
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
+def h2d_probe(gb=4.0):
+    """Host-to-device bandwidth of this machine: one copy of a `gb` GB page-locked
+    buffer into device memory (cudaMemcpyAsync), CUDA events, best of 3; and
+    the host NUMA node of the GPU where sysfs says."""
+    import torch
+    n = int(gb * 1e9) // 8
+    h = torch.empty(n, dtype=torch.float64).pin_memory()
+    d = torch.empty(n, dtype=torch.float64, device="cuda")
+    best = None
+    for _ in range(3):
+        ms = time_call(lambda: d.copy_(h, non_blocking=True), 1, torch.cuda.current_stream())
+        best = ms if best is None else min(best, ms)
+    out = {"h2d_gbs": n * 8 / (best * 1e-3) / 1e9, "probe_gb": n * 8 / 1e9}
+    try:
+        pr = torch.cuda.get_device_properties(0)
+        bus = f"{pr.pci_domain_id:04x}:{pr.pci_bus_id:02x}:{pr.pci_device_id:02x}.0"
+        with open(f"/sys/bus/pci/devices/{bus}/numa_node") as f:
+            out["gpu_numa_node"] = int(f.read().strip())
+    except Exception:
+        pass
+    del h, d
+    torch.cuda.empty_cache()
+    return out
+
+
+def serving_line():
+    """The serving form: a seeded Poisson stream of requests with state
+    dimensions drawn from {4, 6, 12, 24} (m = n/2), F = 0.98 Q, SPD noise
+    covariances, lengths log-uniform in [64, 1,000,000], shipped compactly
+    (model + observations) and expanded on the device at admission; HBM
+    budget 90 GiB; two lanes.  Per precision (FP64, and FP32 + refinement):
+    the capacity served back to back, then 48 requests at each of the offered
+    loads 0.3, 0.6 and 0.9 of it, with p50/p99 latency and throughput."""
+    from ultimate_kalman_gb300 import serve
+    out = {"what": "Poisson request stream, n in {4,6,12,24}, m=n/2, lengths log-uniform [64, 1e6], compact "
+                   "requests expanded on the device, HBM budget 90 GiB, 2 lanes, states; synthetic, seeded"}
+    for name, f32 in (("fp64", False), ("fp32_refine", True)):
+        out[name] = serve.run_loads(requests=48, loads=(0.3, 0.6, 0.9), max_len=1000000, budget_gb=90.0,
+                                    fp32_refine=f32, compact=True, calibration=24, lanes=2)
+    return out
+
+
+def config0_line(stream, with_cpu):
+    """Single constant-velocity track, n=6, m=3, dt=0.1, k=100,000 (prior
+    folded into a square step-0 observation): the odd-even smoother in plain
+    FP64 with covariances and states only, the precision form (states), and
+    the associative smoother in FP64 with covariances.  Errors of every GPU
+    result against the plain FP64 odd-even path are measured here; with
+    with_cpu the oracle's restatement of the reference smoother is timed on
+    the same track (its CPU baseline) and the GPU results are checked
+    against it."""
+    import torch
+    from ultimate_kalman_gb300 import native, problem as pb
+    P = pb.constant_velocity([100000], seed=7)
+    D = native.DeviceProblem(P, covariance=True)
+    runs = {"fp64_states_and_covariances": dict(covariance=True),
+            "fp64_states": dict(covariance=False),
+            "fp32_refine_states": dict(covariance=False, fp32_refine=True, sweeps=1)}
+    out = {"what": "one constant-velocity track, n=6, m=3, k=100000, odd-even smoother (and the associative "
+                   "smoother, FP64 with covariances); synthetic, seeded", "steps": int(P.nsteps)}
+    res = {}
+    for name, kw in runs.items():
+        D.smooth("oddeven", **kw)
+        ms = time_call(lambda: D.smooth("oddeven", stream=stream, **kw), 5, stream)
+        res[name] = (D.state.clone(), D.cov.clone() if kw["covariance"] else None)
+        out[name] = {"ms": ms, "steps_per_s": P.nsteps / (ms * 1e-3)}
+    D.smooth("associative", covariance=True)
+    ms = time_call(lambda: D.smooth("associative", stream=stream, covariance=True), 5, stream)
+    res["assoc"] = (D.state.clone(), D.cov.clone())
+    out["associative_fp64_states_and_covariances"] = {"ms": ms, "steps_per_s": P.nsteps / (ms * 1e-3)}
+    X64, S64 = res["fp64_states_and_covariances"]
+    out["fp32_refine_states"]["rel_err_vs_fp64"] = rel_states(res["fp32_refine_states"][0], X64)
+    out["associative_fp64_states_and_covariances"]["rel_err_vs_fp64_oddeven"] = {
+        "states": rel_states(res["assoc"][0], X64), "covariances": rel_states(res["assoc"][1], S64)}
+    out["speedup_fp32_refine_vs_fp64_states"] = out["fp64_states"]["ms"] / out["fp32_refine_states"]["ms"]
+    if with_cpu:
+        import oracle
+        nt = oracle.max_threads()
+        t0 = time.perf_counter()
+        st, Xo, So = oracle.smooth(P, "oddeven", covariance=True, threads=nt)
+        dt = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        sta, Xa, Sa = oracle.smooth(P, "associative", covariance=True, threads=nt)
+        dta = time.perf_counter() - t0
+        cov_t = lambda S: np.ascontiguousarray(S.cpu().numpy().transpose(0, 2, 1))
+        out["cpu_baseline"] = {
+            "kind": "port", "cores": 1, "unit": UNIT,
+            "oddeven_states_and_covariances": P.nsteps / dt, "associative_states_and_covariances": P.nsteps / dta,
+            "sample": "the whole track; oracle/kalman_oracle.c (one track runs on one thread)",
+            "rel_err_vs_oracle": {
+                "fp64_states": rel_states(X64.cpu().numpy(), Xo), "fp64_covariances": rel_states(cov_t(S64), So),
+                "fp32_refine_states": rel_states(res["fp32_refine_states"][0].cpu().numpy(), Xo),
+                "associative_states": rel_states(res["assoc"][0].cpu().numpy(), Xa),
+                "associative_covariances": rel_states(cov_t(res["assoc"][1]), Sa)}}
+    del D, res
+    torch.cuda.empty_cache()
+    return out
+
+
+def config1_line(stream, with_cpu):
+    """Single track, n=48, m=24, k=1,000,000, F = 0.99 Q, G ~ N(0, 1/m), SPD
+    noise covariances with eigenvalues in [0.1, 1], 5 % of steps unobserved;
+    its 93 GB of per-step equations are written on the device by the
+    equation builder.  The associative smoother (FP64, states and
+    covariances), the odd-even smoother (FP64 with covariances) and the
+    precision form (states), each timed once after a warm-up; errors against
+    the FP64 odd-even result.  With with_cpu the oracle runs on a 3,000-step
+    track of the same shape and the GPU smoothers are checked against it."""
+    import torch
+    from ultimate_kalman_gb300 import native, shapes
+    k = 1000000
+    D = shapes.device_track(k, 48, 24, missing=0.05, covariance=True)
+    out = {"what": "one track n=48, m=24, k=1000000, F = 0.99 Q, G ~ N(0, 1/m), noise covariance eigenvalues "
+                   "U[0.1, 1], 5 % unobserved; equations built on the device; synthetic, seeded",
+           "input_gb": D.input_bytes() / 1e9}
+    runs = [("oddeven_fp64_states_and_covariances", "oddeven", dict(covariance=True)),
+            ("associative_fp64_states_and_covariances", "associative", dict(covariance=True)),
+            ("oddeven_fp32_refine_states", "oddeven", dict(covariance=False, fp32_refine=True, sweeps=1))]
+    ref = None  # the FP64 odd-even states and every 50th covariance block (HBM: 93 GB inputs + workspace)
+    for name, alg, kw in runs:
+        D.smooth(alg, **kw)
+        ms = time_call(lambda: D.smooth(alg, stream=stream, **kw), 1, stream)
+        out[name] = {"ms": ms, "steps_per_s": k / (ms * 1e-3)}
+        if ref is None:
+            ref = (D.state.clone(), D.cov[::50].clone())
+        elif kw["covariance"]:
+            out[name]["rel_err_vs_fp64_oddeven"] = {"states": rel_states(D.state, ref[0]),
+                                                    "covariances_every_50th_step": rel_states(D.cov[::50], ref[1])}
+        else:
+            out[name]["rel_err_vs_fp64"] = rel_states(D.state, ref[0])
+        native.release()
+    del D, ref
+    torch.cuda.empty_cache()
+    if with_cpu:
+        import oracle
+        ks = 3000
+        P = shapes.synthetic_track(ks, 48, 24, missing=0.05)
+        Ds = native.DeviceProblem(P, covariance=True)
+        got = {}
+        for alg, kw in (("associative", dict(covariance=True)), ("oddeven", dict(covariance=True)),
+                        ("fp32", dict(covariance=False, fp32_refine=True, sweeps=1))):
+            Ds.smooth("oddeven" if alg == "fp32" else alg, **kw)
+            X, S = Ds.results()
+            got[alg] = (X, S if kw["covariance"] else None)
+        t0 = time.perf_counter()
+        _, Xoe, Soe = oracle.smooth(P, "oddeven", covariance=True)
+        dto = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        _, Xas, Sas = oracle.smooth(P, "associative", covariance=True)
+        dta = time.perf_counter() - t0
+        out["cpu_baseline"] = {
+            "kind": "port", "cores": 1, "unit": UNIT, "oddeven_states_and_covariances": ks / dto,
+            "associative_states_and_covariances": ks / dta,
+            "sample": f"a {ks}-step track of the same shape and distribution; oracle/kalman_oracle.c, one thread",
+            "rel_err_vs_oracle": {
+                "oddeven_fp64_states": rel_states(got["oddeven"][0], Xoe),
+                "oddeven_fp64_covariances": rel_states(got["oddeven"][1], Soe),
+                "associative_fp64_states": rel_states(got["associative"][0], Xas),
+                "associative_fp64_covariances": rel_states(got["associative"][1], Sas),
+                "fp32_refine_states": rel_states(got["fp32"][0], Xoe)}}
+        del Ds
+        torch.cuda.empty_cache()
     return out
 
 

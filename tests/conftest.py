@@ -1,6 +1,7 @@
 """Shared fixtures.  Tests marked ``gpu`` need a CUDA device; the rest run on
 CPU.  The oracle package (test infrastructure) is importable from here."""
 import glob
+import json
 import os
 import sys
 
@@ -30,3 +31,27 @@ def load_golden(path):
 @pytest.fixture(params=GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
 def golden(request):
     return load_golden(request.param)
+
+
+_PARITY = []
+
+
+@pytest.fixture(scope="session")
+def parity_log():
+    """record(case, **errors): keeps the achieved relative errors of a parity
+    test; at the end of the session they are printed and, when the
+    environment names a file in UKG_PARITY_LOG, written there as JSON."""
+    def record(case, **errors):
+        _PARITY.append({"case": case, **{k: float(v) for k, v in errors.items()}})
+    yield record
+    if _PARITY:
+        worst = {}
+        for r in _PARITY:
+            for k, v in r.items():
+                if k != "case":
+                    worst[k] = max(worst.get(k, 0.0), v)
+        print("\nachieved relative errors (max over cases):", json.dumps(worst))
+        path = os.environ.get("UKG_PARITY_LOG")
+        if path:
+            with open(path, "w") as f:
+                json.dump({"worst": worst, "cases": _PARITY}, f, indent=1)

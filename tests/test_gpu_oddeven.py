@@ -166,3 +166,40 @@ def test_cta_path_every_length_1_to_17(fp32):
     else:
         X, S = native.smooth(P)
         check(P, X, S)
+
+
+def test_concurrent_host_threads_with_different_shapes():
+    """Host threads smoothing problems of different state dimensions at the
+    same time, each on its own stream (the serving lanes): every call
+    succeeds and equals the same problem smoothed alone, bit for bit.  The
+    FP64 kernels shared between shapes need different amounts of dynamic
+    shared memory, so a per-call kernel attribute would race here."""
+    import threading
+    import torch
+    probs = {4: pb.random_dynamics([3000, 17], 4, 2, seed=41), 6: pb.constant_velocity([2500, 33], seed=42),
+             5: pb.random_dynamics([2000, 9], 5, 3, seed=43)}
+    alone = {n: native.smooth(P, "oddeven", covariance=True) for n, P in probs.items()}
+    errors, results = [], {}
+
+    def work(n):
+        try:
+            torch.cuda.set_device(0)
+            st = torch.cuda.Stream()
+            D = native.DeviceProblem(probs[n], covariance=True)
+            for _ in range(20):
+                with torch.cuda.stream(st):
+                    D.smooth("oddeven", covariance=True, stream=st)
+            torch.cuda.synchronize()
+            results[n] = D.results()
+        except Exception as e:  # reported below
+            errors.append(f"n={n}: {e}")
+
+    threads = [threading.Thread(target=work, args=(n,)) for n in probs]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    for n, (X, S) in results.items():
+        np.testing.assert_array_equal(X, alone[n][0])
+        np.testing.assert_array_equal(S, alone[n][1])

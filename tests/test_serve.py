@@ -1,20 +1,37 @@
 """The serving loop (ultimate_kalman_gb300/serve.py): scheduling rules on a
 simulated clock (CPU), and on the GPU, results of requests served in mixed
-batches equal the same requests smoothed alone (bit-equal: tracks are
-independent, so a batch does not change a track's arithmetic)."""
+batches -- with batches of other requests running beside them on other lanes
+-- equal the same requests smoothed alone (bit-equal: tracks are independent,
+so neither a batch nor what overlaps it changes a track's arithmetic)."""
 import numpy as np
 import pytest
 
 from ultimate_kalman_gb300 import serve
 
 
-class FakeExecutor:
-    """Records uploads and batches; the clock advances by the batch's steps."""
+class FakeFuture:
+    def __init__(self, clock, finish):
+        self.clock, self.finish = clock, finish
 
-    def __init__(self, clock, rate=1e6):
-        self.clock, self.rate = clock, rate
+    def done(self):
+        return self.clock.t >= self.finish
+
+    def result(self):
+        return None
+
+    def eta(self):
+        return max(0.0, self.finish - self.clock.t)
+
+
+class FakeExecutor:
+    """Records uploads and batches; a batch finishes after its steps / rate
+    on the simulated clock, and `lanes` batches may run at once."""
+
+    def __init__(self, clock, rate=1e6, lanes=1):
+        self.clock, self.rate, self.lanes = clock, rate, lanes
         self.resident = set()
         self.batches = []
+        self.running = []  # (start, finish) of every batch
 
     def upload(self, r):
         self.resident.add(r.rid)
@@ -22,12 +39,14 @@ class FakeExecutor:
     def release(self, r):
         self.resident.discard(r.rid)
 
-    def run(self, batch):
+    def launch(self, batch, lane):
         assert all(r.rid in self.resident for r in batch)
         self.batches.append([r.rid for r in batch])
-        self.clock.t += sum(r.steps for r in batch) / self.rate
+        finish = self.clock.t + sum(r.steps for r in batch) / self.rate
+        self.running.append((self.clock.t, finish))
         for r in batch:
             r.state = np.zeros((r.steps, r.problem.n))
+        return FakeFuture(self.clock, finish)
 
 
 class Clock:
@@ -94,6 +113,36 @@ def test_request_larger_than_the_budget_is_refused():
         srv.serve(reqs)
 
 
+def test_lanes_admit_and_start_batches_while_others_run():
+    """With two lanes a second batch starts before the first one finishes, and
+    requests that arrive meanwhile are admitted (not held until the GPU is
+    idle)."""
+    clock = Clock()
+    reqs = make_stream(nreq=40, rate=400.0, seed=4)
+    ex = FakeExecutor(clock, rate=5e4, lanes=2)
+    srv = serve.Server(ex, hbm_budget=1 << 40, clock=clock, wait=clock.wait)
+    done = srv.serve(reqs)
+    assert len(done) == len(reqs)
+    assert srv.max_running == 2
+    iv = sorted(ex.running)
+    assert any(b[0] < a[1] for a, b in zip(iv, iv[1:]))  # some batches overlapped
+    admitted_while_busy = [r for r in done if any(a < r.admitted < b for a, b in iv)]
+    assert admitted_while_busy
+
+
+def test_footprint_counts_the_library_workspace():
+    r = make_stream(nreq=1)[0]
+    base = serve.footprint(r)
+    r.workspace = 12345
+    assert serve.footprint(r) == base + 12345
+
+
+def test_device_overlap_measure():
+    assert serve.device_overlap([(0, 0.0, 1.0, []), (1, 1.0, 2.0, [])]) == 1.0
+    assert serve.device_overlap([(0, 0.0, 2.0, []), (1, 0.0, 2.0, [])]) == 2.0
+    assert serve.device_overlap([(0, 0.0, 2.0, []), (1, 1.0, 3.0, [])]) == pytest.approx(4.0 / 3.0)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("fp32", [False, True])
 def test_served_results_equal_results_alone(fp32):
@@ -102,13 +151,75 @@ def test_served_results_equal_results_alone(fp32):
         pytest.skip("needs a CUDA device")
     from ultimate_kalman_gb300 import native
     reqs = serve.request_stream(24, 1e6, seed=11, dims=(4, 6, 12), min_len=64, max_len=3000, fp32_refine=fp32)
-    ex = serve.GpuExecutor()
+    ex = serve.GpuExecutor(lanes=2)
     srv = serve.Server(ex, hbm_budget=1 << 32)
     done = srv.serve(reqs)
+    ex.close()
     assert len(srv.batches) < len(reqs)  # some requests shared a batch
     for r in done:
         X, _ = native.smooth(r.problem, covariance=False, fp32_refine=fp32)
         np.testing.assert_array_equal(r.state, X)
+
+
+@pytest.mark.gpu
+def test_two_batches_in_flight_overlap_on_the_device_and_match_alone():
+    """Requests of two shape classes arrive together; with two lanes both
+    batches are on the GPU at once (their device intervals intersect) and every
+    result equals the request smoothed alone, bit for bit."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    from ultimate_kalman_gb300 import native
+    rng = np.random.default_rng(21)
+    problems = [serve.serving_track(40000 if n == 12 else 60000, n, n // 2, rng) for n in [12, 6, 12, 6, 12, 6]]
+    ex = serve.GpuExecutor(lanes=2)
+    for _ in range(2):  # the first pass warms the lanes (workspaces, kernel loading), the second is checked
+        reqs = [serve.Request(i, 0.0, P, covariance=(P.n == 6)) for i, P in enumerate(problems)]
+        ex.intervals.clear()
+        srv = serve.Server(ex, hbm_budget=1 << 36, max_batch_steps=80000)
+        done = srv.serve(reqs)
+    ex.close()
+    assert srv.max_running == 2
+    iv = sorted((a, b) for _, a, b, _ in ex.intervals)
+    assert any(b[0] < a[1] for a, b in zip(iv, iv[1:])), iv
+    assert serve.device_overlap(ex.intervals) > 1.0
+    for r in done:
+        X, S = native.smooth(r.problem, covariance=r.covariance)
+        np.testing.assert_array_equal(r.state, X)
+        if r.covariance:
+            np.testing.assert_array_equal(r.cov, S)
+
+
+@pytest.mark.gpu
+def test_library_workspace_figure_is_what_a_call_holds():
+    """kalman_gpu_oddeven_workspace_bytes equals the workspace a fresh host
+    thread holds after smoothing the problem (per-thread and CTA kernels, FP64
+    and the precision form)."""
+    import threading
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    from ultimate_kalman_gb300 import native, problem as pb
+    cases = [(pb.constant_velocity([300, 41], seed=1), dict(covariance=True)),
+             (pb.constant_velocity([300, 41], seed=1), dict(covariance=False, fp32_refine=True)),
+             (pb.random_dynamics([200, 33], 12, 6, seed=2), dict(covariance=True)),
+             (pb.random_dynamics([200, 33], 12, 6, seed=2), dict(covariance=False, fp32_refine=True))]
+    for P, kw in cases:
+        D = native.DeviceProblem(P, covariance=kw["covariance"])
+        got = {}
+
+        def work():
+            torch.cuda.set_device(0)
+            D.smooth("oddeven", **kw)
+            torch.cuda.synchronize()
+            got["held"] = native.workspace_held()
+            native.release()
+
+        th = threading.Thread(target=work)
+        th.start()
+        th.join()
+        want = native.oddeven_workspace_bytes(D.struct, **kw)
+        assert want > 0 and got["held"] == want, (P.n, kw, got, want)
 
 
 def test_compact_requests_expand_to_the_packed_track():
@@ -139,6 +250,7 @@ def test_compact_requests_served_equal_packed_alone():
     ex = serve.GpuExecutor()
     srv = serve.Server(ex, hbm_budget=1 << 32)
     done = srv.serve(reqs)
+    ex.close()
     for r in done:
         X, _ = native.smooth(r.problem.to_packed(), covariance=False)
         np.testing.assert_array_equal(r.state, X)

@@ -34,7 +34,9 @@ def _compile(src, verbose):
     out = os.path.join(BUILD, os.path.basename(src) + ".o")
     inc = ["-I", os.path.join(REPO, "include"), "-I", CSRC]
     if src.endswith(".cu"):
-        cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *inc, "-c", src, "-o", out]
+        # --split-compile=0: nvcc optimizes the translation unit's kernels in parallel on every core
+        cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "--split-compile=0", "-Xcompiler", "-fPIC", *inc,
+               "-c", src, "-o", out]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
     elif src.endswith(".cpp"):

@@ -788,17 +788,20 @@ struct Workspace {
 };
 thread_local Workspace tl_ws;
 
-int ensure(size_t bytes, void** out)
+/* grows by stream-ordered allocation on the call's stream, which does not
+ * synchronize the device (see ensure_workspace in oddeven.cu)               */
+int ensure(size_t bytes, void** out, cudaStream_t st)
 {
   int dev = 0;
   cudaGetDevice(&dev);
   if (tl_ws.dev && (tl_ws.bytes < bytes || tl_ws.device != dev)) {
-    cudaFree(tl_ws.dev);
+    if (tl_ws.device == dev) cudaFreeAsync(tl_ws.dev, st);
+    else cudaFree(tl_ws.dev);
     tl_ws = Workspace();
   }
   if (!tl_ws.dev) {
     size_t want = bytes + (bytes >> 3);
-    if (cudaMalloc(&tl_ws.dev, want) != cudaSuccess) {
+    if (cudaMallocAsync(&tl_ws.dev, want, st) != cudaSuccess) {
       cudaGetLastError();
       tl_ws = Workspace();
       return ukg_set_error(KALMAN_GPU_ENOMEM, "cudaMalloc of %zu bytes of workspace failed", want);
@@ -898,6 +901,8 @@ int finish(cudaStream_t st, int* dflag)
 
 }  // namespace
 
+extern "C" int64_t ukg_associative_workspace_held(void) { return (int64_t)tl_ws.bytes; }
+
 extern "C" void ukg_release_associative_workspace(void)
 {
   if (tl_ws.dev) cudaFree(tl_ws.dev);
@@ -960,7 +965,7 @@ extern "C" int ukg_associative_device(uint32_t options, const kalman_gpu_problem
     o_scratch = take((size_t)ncta * per_cta * sizeof(double));
   }
   void* base = nullptr;
-  if (int e = ensure(bytes, &base)) return e;
+  if (int e = ensure(bytes, &base, st)) return e;
   char* B = (char*)base;
   int64_t* dtab = (int64_t*)(B + o_tab);
   int* dflag = (int*)(B + o_flag);
@@ -1083,12 +1088,12 @@ extern "C" int ukg_associative_device(uint32_t options, const kalman_gpu_problem
   if (pick_block(pt_elem, 64, &be) || pick_block(pt_comb, 64, &bc) || pick_block(pt_selem, 64, &bsm))
     return ukg_set_error(KALMAN_GPU_EINVAL, "state dimension %d needs more shared memory per thread than this build "
                          "of the associative kernels uses", n);
-  cudaFuncSetAttribute(element_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(be * pt_elem));
-  cudaFuncSetAttribute(up_kernel<FElems>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bc * pt_comb));
-  cudaFuncSetAttribute(down_kernel<FElems>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bc * pt_comb));
-  cudaFuncSetAttribute(up_kernel<SElems>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bc * pt_comb));
-  cudaFuncSetAttribute(down_kernel<SElems>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bc * pt_comb));
-  cudaFuncSetAttribute(smooth_element_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bsm * pt_selem));
+  ukg_allow_dynamic_smem((const void*)element_kernel);
+  ukg_allow_dynamic_smem((const void*)up_kernel<FElems>);
+  ukg_allow_dynamic_smem((const void*)down_kernel<FElems>);
+  ukg_allow_dynamic_smem((const void*)up_kernel<SElems>);
+  ukg_allow_dynamic_smem((const void*)down_kernel<SElems>);
+  ukg_allow_dynamic_smem((const void*)smooth_element_kernel);
   auto grid = [](int64_t items, int block) { return (unsigned)((items + block - 1) / block); };
   const int ew = 128;
 

@@ -172,4 +172,65 @@ __device__ __forceinline__ df sqrt(df a)
   return fast_two_sum(s0, __fmul_rn(res, __fdividef(0.5f, s0)));
 }
 
+/* ---------------------------------------------------------------------------
+ * dd: a double-float number as a value type, so that kernels written for a
+ * scalar type T (fma, sqrt, copysign, T(0), T(1) / x, comparisons) compile
+ * unchanged with T = dd and run their FP64 algorithm on the FP32 pipe with
+ * about 47 significant bits.  8 bytes, 8-byte aligned: the same footprint as
+ * FP64 in every array and shared-memory slice.  Values stay normalized
+ * (|lo| <= ulp(hi) / 2), so equality with zero is a test of hi.
+ * ------------------------------------------------------------------------ */
+struct __align__(8) dd {
+  float hi, lo;
+  dd() = default;
+  __host__ __device__ constexpr dd(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr dd(int v) : hi((float)v), lo(0.0f) {}
+  __host__ __device__ constexpr dd(float v) : hi(v), lo(0.0f) {}
+  __device__ __forceinline__ dd(df a) : hi(a.hi), lo(a.lo) {}
+  __device__ __forceinline__ dd(double x) : dd(split(x)) {} /* the exact leading 47 bits */
+  __device__ __forceinline__ operator df() const { return df{hi, lo}; }
+};
+
+__device__ __forceinline__ dd operator+(dd a, dd b) { return add(a, b); }
+__device__ __forceinline__ dd operator-(dd a, dd b) { return add(a, neg(b)); }
+__device__ __forceinline__ dd operator-(dd a) { return dd(-a.hi, -a.lo); }
+__device__ __forceinline__ dd operator*(dd a, dd b) { return mul(a, b); }
+/* a / b = a * (1 / b), the reciprocal by one Newton step (rcp above)        */
+__device__ __forceinline__ dd operator/(dd a, dd b) { return mul(a, rcp(b)); }
+__device__ __forceinline__ dd& operator+=(dd& a, dd b) { return a = a + b; }
+__device__ __forceinline__ dd& operator-=(dd& a, dd b) { return a = a - b; }
+__device__ __forceinline__ dd& operator*=(dd& a, dd b) { return a = a * b; }
+__device__ __forceinline__ dd& operator/=(dd& a, dd b) { return a = a / b; }
+__device__ __forceinline__ bool operator==(dd a, dd b) { return a.hi == b.hi && a.lo == b.lo; }
+__device__ __forceinline__ bool operator!=(dd a, dd b) { return !(a == b); }
+__device__ __forceinline__ bool operator<(dd a, dd b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool operator>(dd a, dd b) { return b < a; }
+__device__ __forceinline__ bool operator<=(dd a, dd b) { return !(b < a); }
+__device__ __forceinline__ bool operator>=(dd a, dd b) { return !(a < b); }
+__device__ __forceinline__ dd fma(dd a, dd b, dd c) { return fma(df(a), df(b), df(c)); }
+__device__ __forceinline__ dd fabs(dd a) { return a.hi < 0.0f ? -a : a; }
+__device__ __forceinline__ dd copysign(dd a, dd b)
+{
+  return (signbit(a.hi) != signbit(b.hi)) ? -a : a;
+}
+/* the Newton step needs a positive argument; 0 (and negative or NaN
+ * arguments) take the FP32 square root's value                             */
+__device__ __forceinline__ dd sqrt(dd a) { return a.hi > 0.0f ? dd(sqrt(df(a))) : dd(sqrtf(a.hi), 0.0f); }
+
+/* warp shuffle of both parts (found by argument-dependent lookup where
+ * kernels shuffle a T)                                                      */
+__device__ __forceinline__ dd __shfl_xor_sync(unsigned mask, dd v, int lane_mask)
+{
+  return dd(::__shfl_xor_sync(mask, v.hi, lane_mask), ::__shfl_xor_sync(mask, v.lo, lane_mask));
+}
+
+template <>
+__device__ __forceinline__ dd narrow<dd>(double x) { return dd(split(x)); }
+__device__ __forceinline__ double widen(dd x) { return join(df(x)); }
+/* an output value as FP64: the plain conversion for float and double, the
+ * sum of the parts for dd                                                   */
+template <typename T>
+__device__ __forceinline__ double to_f64(T x) { return (double)x; }
+__device__ __forceinline__ double to_f64(dd x) { return join(df(x)); }
+
 } /* namespace ukg_df */

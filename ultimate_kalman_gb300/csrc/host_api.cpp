@@ -29,6 +29,8 @@
 #include <cstring>
 #include <ctime>
 #include <deque>
+#include <mutex>
+#include <set>
 #include <vector>
 
 #include "ukgpu_internal.h"
@@ -282,6 +284,33 @@ extern "C" int kalman_gpu_smooth_associative_packed(uint32_t options, const kalm
 
 extern "C" void ukg_release_oddeven_workspace(void);
 extern "C" void ukg_release_associative_workspace(void);
+extern "C" int64_t ukg_oddeven_workspace_held(void);
+extern "C" int64_t ukg_associative_workspace_held(void);
+
+extern "C" void ukg_allow_dynamic_smem(const void* kernel)
+{
+  static std::mutex mu;
+  static std::set<std::pair<int, const void*>> done;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!done.insert({dev, kernel}).second) return;
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  int stat = 0;
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, kernel) == cudaSuccess) stat = (int)fa.sharedSizeBytes;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - stat);
+  cudaGetLastError();
+}
+
+extern "C" int64_t kalman_gpu_workspace_held(void)
+{
+  return ukg_oddeven_workspace_held() + ukg_associative_workspace_held() + (int64_t)tl_stage.bytes;
+}
 
 extern "C" void kalman_gpu_release(void)
 {

@@ -62,6 +62,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "profiling.h"
@@ -2592,18 +2593,20 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
   const Kernels<T> K = choose_kernels<T>(n, mx);
   if (K.bp) bp = K.bp;
   if (K.bs) bs = K.bs;
-  cudaFuncSetAttribute(weigh_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bw * pt_weigh));
+  ukg_allow_dynamic_smem((const void*)weigh_kernel<T>);
   if (staged)
-    cudaFuncSetAttribute(weigh_staged_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)weigh_smem);
+    ukg_allow_dynamic_smem((const void*)weigh_staged_kernel<T>);
   const size_t pair_smem = K.pair_smem ? K.pair_smem : bp * pt_pair;
-  cudaFuncSetAttribute(K.pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pair_smem);
-  cudaFuncSetAttribute(tail_kernel<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bt * pt_tail));
-  cudaFuncSetAttribute(K.solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(bs * pt_solve));
-  cudaFuncSetAttribute(residual_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(br * pt_res));
+  ukg_allow_dynamic_smem((const void*)K.pair);
+  ukg_allow_dynamic_smem((const void*)tail_kernel<T, T>);
+  ukg_allow_dynamic_smem((const void*)K.solve);
+  ukg_allow_dynamic_smem((const void*)residual_kernel);
 
   auto grid = [](int64_t items, int block) { return (unsigned)((items + block - 1) / block); };
-  const int kPair = P.fp32 ? UKG_K_PAIR32 : UKG_K_PAIR;
-  const int kSolve = P.fp32 ? UKG_K_SOLVE32 : UKG_K_SOLVE;
+  constexpr bool kDD = std::is_same<T, ukg_df::dd>::value; /* double-float: own kernel classes */
+  const int kWeigh = kDD ? UKG_K_DF_WEIGH : UKG_K_WEIGH, kTail = kDD ? UKG_K_DF_TAIL : UKG_K_TAIL;
+  const int kPair = P.fp32 ? UKG_K_PAIR32 : kDD ? UKG_K_DF_PAIR : UKG_K_PAIR;
+  const int kSolve = P.fp32 ? UKG_K_SOLVE32 : kDD ? UKG_K_DF_SOLVE : UKG_K_SOLVE;
   Soa<T> baseR{P.refine ? (T*)(B + P.o_baseR) : nullptr, std::max(T_, 1)};
 
   /* double-float level-0 weighing and refinement residual where compiled */
@@ -2633,7 +2636,7 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
     if constexpr (sizeof(T) == sizeof(float)) {
       const size_t smem_df = 16 + (size_t)kWeighBS * blk * sizeof(double);
       if (DK.weigh && smem_df <= (size_t)optin) {
-        cudaFuncSetAttribute(DK.weigh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_df);
+        ukg_allow_dynamic_smem((const void*)DK.weigh);
         UKG_LAUNCH(UKG_K_WEIGH, st,
                    (DK.weigh<<<grid(p->nsteps, kWeighBS), kWeighBS, smem_df, st>>>(w, eq0lo, raw, p->nsteps,
                                                                                     (align_bits & 15) == 0)));
@@ -2646,8 +2649,7 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
                  (weigh_staged_kernel<T><<<grid(p->nsteps, kWeighBS), kWeighBS, weigh_smem, st>>>(w, raw, p->nsteps,
                                                                                                    blk)));
     else
-      UKG_LAUNCH(UKG_K_WEIGH, st,
-                 (weigh_kernel<T><<<grid(p->nsteps, bw), bw, bw * pt_weigh, st>>>(w, raw, p->nsteps)));
+      UKG_LAUNCH(kWeigh, st, (weigh_kernel<T><<<grid(p->nsteps, bw), bw, bw * pt_weigh, st>>>(w, raw, p->nsteps)));
   }
   auto common = [&](auto& a, int l) {
     a.ct = tables(l);
@@ -2684,7 +2686,7 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
         }
       }
       if (!done)
-        UKG_LAUNCH(UKG_K_TAIL, st, (tail_kernel<T, T><<<grid(lp[l].ntail, bt), bt, bt * pt_tail, st>>>(a)));
+        UKG_LAUNCH(kTail, st, (tail_kernel<T, T><<<grid(lp[l].ntail, bt), bt, bt * pt_tail, st>>>(a)));
     }
   }
   /* ---- back-substitution ---- */
@@ -2820,19 +2822,25 @@ int ensure_mapped_tables(size_t entries)
   return 0;
 }
 
-int ensure_workspace(size_t bytes, void** out)
+/* The workspace grows by stream-ordered allocation on the call's stream
+ * (cudaFreeAsync / cudaMallocAsync): cudaFree and cudaMalloc synchronize the
+ * whole device, which would stall the calls other host threads have running
+ * on their own streams.  Every call synchronizes its stream before returning,
+ * so the next call, on any stream, finds the allocation complete.           */
+int ensure_workspace(size_t bytes, void** out, cudaStream_t st)
 {
   int dev = 0;
   cudaGetDevice(&dev);
   Workspace& w = tl_ws;
   if (w.dev && (w.dev_bytes < bytes || w.device != dev)) {
-    cudaFree(w.dev);
+    if (w.device == dev) cudaFreeAsync(w.dev, st);
+    else cudaFree(w.dev);
     w.dev = nullptr;
     w.dev_bytes = 0;
   }
   if (!w.dev) {
     size_t want = bytes + (bytes >> 3);
-    cudaError_t e = cudaMalloc(&w.dev, want);
+    cudaError_t e = cudaMallocAsync(&w.dev, want, st);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return ukg_set_error(KALMAN_GPU_ENOMEM, "cudaMalloc of %zu bytes of workspace failed: %s", want,
@@ -2964,6 +2972,8 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
     a.baseR = baseR;
   };
   auto grid = [&](int64_t items) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(items, ncta)); };
+  constexpr bool kDD = std::is_same<T, ukg_df::dd>::value; /* double-float: own kernel classes */
+  const int kWeigh = kDD ? UKG_K_DF_WEIGH : UKG_K_WEIGH, kTail = kDD ? UKG_K_DF_TAIL : UKG_K_TAIL;
   const ctak::RawA raw{p->H, p->F, p->c, p->K, p->G, p->o, p->C, p->K_type, p->C_type, p->obs_rows, p->mmax};
   {
     ctak::CArgs<T> a;
@@ -2976,12 +2986,13 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
     if (2 * wneed <= a.scratch_per_cta) {
       a.scratch_per_cta /= 2;
       const unsigned g2 = (unsigned)std::max<int64_t>(1, std::min<int64_t>(p->nsteps, 2 * (int64_t)ncta));
-      UKG_LAUNCH(UKG_K_WEIGH, st, (ctak::weigh_cta<T><<<g2, cta::NT, 0, st>>>(a, raw, p->nsteps)));
+      UKG_LAUNCH(kWeigh, st, (ctak::weigh_cta<T><<<g2, cta::NT, 0, st>>>(a, raw, p->nsteps)));
     } else {
-      UKG_LAUNCH(UKG_K_WEIGH, st, (ctak::weigh_cta<T><<<grid(p->nsteps), cta::NT, 0, st>>>(a, raw, p->nsteps)));
+      UKG_LAUNCH(kWeigh, st, (ctak::weigh_cta<T><<<grid(p->nsteps), cta::NT, 0, st>>>(a, raw, p->nsteps)));
     }
   }
-  const int kPair = P.fp32 ? UKG_K_PAIR32 : UKG_K_PAIR, kSolve = P.fp32 ? UKG_K_SOLVE32 : UKG_K_SOLVE;
+  const int kPair = P.fp32 ? UKG_K_PAIR32 : kDD ? UKG_K_DF_PAIR : UKG_K_PAIR;
+  const int kSolve = P.fp32 ? UKG_K_SOLVE32 : kDD ? UKG_K_DF_SOLVE : UKG_K_SOLVE;
   /* 3xTF32 tensor-core trailing updates in the FP32 blocked QR (an option) */
   constexpr bool kF32 = sizeof(T) == sizeof(float);
   const bool tc = kF32 && (options & KALMAN_GPU_TF32X3) != 0;
@@ -3004,9 +3015,9 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
         if constexpr (kF32)
           UKG_LAUNCH(UKG_K_TAIL, st, (ctak::tail_cta<T, true, true><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
       } else if (n >= cta::kBlockedMinN)
-        UKG_LAUNCH(UKG_K_TAIL, st, (ctak::tail_cta<T, true><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
+        UKG_LAUNCH(kTail, st, (ctak::tail_cta<T, true><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
       else
-        UKG_LAUNCH(UKG_K_TAIL, st, (ctak::tail_cta<T, false><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
+        UKG_LAUNCH(kTail, st, (ctak::tail_cta<T, false><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
     }
   }
   for (int l = nlev - 2; l >= 0; --l) {
@@ -3112,7 +3123,8 @@ extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* 
     if (mxp > kCtaMaxN)
       return ukg_set_error(KALMAN_GPU_EINVAL, "state dimension %d (observation rows %d) above this build's limit %d",
                            p->n, p->mmax, kCtaMaxN);
-    const bool f32 = (options & KALMAN_GPU_FP32_REFINE) != 0;
+    const bool dd = (options & KALMAN_GPU_FP32_REFINE) && want_cov; /* double-float with covariances */
+    const bool f32 = (options & KALMAN_GPU_FP32_REFINE) && !dd;
     Plan P;
     const size_t need = build_plan(p, want_cov, f32, f32, P, nullptr, 0);
     if (need == 0) return ukg_set_error(KALMAN_GPU_EINVAL, "tracks longer than 2^%d steps", kMaxLevels - 1);
@@ -3122,14 +3134,19 @@ extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* 
     const int64_t per = cta_scratch_per_cta(p->n, p->mmax);
     const size_t scratch_off = align_up(P.bytes, 256);
     void* base = nullptr;
-    if (int e = ensure_workspace(scratch_off + (size_t)ncta * per * sizeof(double), &base)) return e;
+    if (int e = ensure_workspace(scratch_off + (size_t)ncta * per * sizeof(double), &base, (cudaStream_t)cuda_stream))
+      return e;
     if (f32)
       return run_plan_cta<float>(options, p, (cudaStream_t)cuda_stream, P, tl_mtab.dev, (char*)base,
                                  (char*)base + scratch_off, per, ncta);
+    if (dd)
+      return run_plan_cta<ukg_df::dd>(options, p, (cudaStream_t)cuda_stream, P, tl_mtab.dev, (char*)base,
+                                      (char*)base + scratch_off, per, ncta);
     return run_plan_cta<double>(options, p, (cudaStream_t)cuda_stream, P, tl_mtab.dev, (char*)base,
                                 (char*)base + scratch_off, per, ncta);
   }
-  const bool fp32 = (options & KALMAN_GPU_FP32_REFINE) != 0;
+  const bool dd = (options & KALMAN_GPU_FP32_REFINE) && want_cov; /* double-float with covariances */
+  const bool fp32 = (options & KALMAN_GPU_FP32_REFINE) && !dd;
   Plan P;
   const size_t need = build_plan(p, want_cov, fp32, fp32, P, nullptr, 0);
   if (need == 0) return ukg_set_error(KALMAN_GPU_EINVAL, "tracks longer than 2^%d steps", kMaxLevels - 1);
@@ -3137,8 +3154,9 @@ extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* 
   int64_t* tab = tl_mtab.host;
   build_plan(p, want_cov, fp32, fp32, P, tab, need);
   void* base = nullptr;
-  if (int e = ensure_workspace(P.bytes, &base)) return e;
+  if (int e = ensure_workspace(P.bytes, &base, (cudaStream_t)cuda_stream)) return e;
   if (fp32) return run_plan<float>(options, p, (cudaStream_t)cuda_stream, P, tab, (char*)base, tl_mtab.dev);
+  if (dd) return run_plan<ukg_df::dd>(options, p, (cudaStream_t)cuda_stream, P, tab, (char*)base, tl_mtab.dev);
   return run_plan<double>(options, p, (cudaStream_t)cuda_stream, P, tab, (char*)base, tl_mtab.dev);
 }
 
@@ -3152,7 +3170,7 @@ extern "C" int64_t kalman_gpu_oddeven_workspace_bytes(uint32_t options, const ka
   if (ukg_validate_problem(p, 0)) return -1;
   if (p->nsteps == 0) return 0;
   const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
-  const bool f32 = (options & KALMAN_GPU_FP32_REFINE) != 0;
+  const bool f32 = (options & KALMAN_GPU_FP32_REFINE) && !want_cov; /* with covariances: double-float, 8 bytes */
   const int mxp = p->mmax > p->n ? p->mmax : p->n;
   Plan P;
   if (build_plan(p, want_cov, f32, f32, P, nullptr, 0) == 0) {
@@ -3309,7 +3327,8 @@ extern "C" kalman_gpu_plan_t* kalman_gpu_plan_create(uint32_t options, const kal
                   p->mmax, kCtaMaxN);
     return nullptr;
   }
-  const bool fp32 = (options & KALMAN_GPU_FP32_REFINE) != 0;
+  const bool dd = (options & KALMAN_GPU_FP32_REFINE) && want_cov; /* double-float with covariances */
+  const bool fp32 = (options & KALMAN_GPU_FP32_REFINE) && !dd;
   Plan P;
   const size_t need = build_plan(p, want_cov, fp32, fp32, P, nullptr, 0);
   if (need == 0) {
@@ -3344,6 +3363,11 @@ extern "C" kalman_gpu_plan_t* kalman_gpu_plan_create(uint32_t options, const kal
     if (cta && fp32)
       st = run_plan_cta<float>(options, p, cs, P, nullptr, (char*)pl->work, (char*)pl->work + scratch_off, per, ncta,
                                true);
+    else if (cta && dd)
+      st = run_plan_cta<ukg_df::dd>(options, p, cs, P, nullptr, (char*)pl->work, (char*)pl->work + scratch_off, per,
+                                    ncta, true);
+    else if (dd)
+      st = run_plan<ukg_df::dd>(options, p, cs, P, nullptr, (char*)pl->work, nullptr, true);
     else if (cta)
       st = run_plan_cta<double>(options, p, cs, P, nullptr, (char*)pl->work, (char*)pl->work + scratch_off, per, ncta,
                                 true);

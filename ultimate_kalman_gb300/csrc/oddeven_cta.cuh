@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs<T> a)
           const int r = e / n, c = e - r * n;
           T s = T(0);
           for (int k = (r > c ? r : c); k < n; ++k) s = fma(Ri[(int64_t)r * n + k], Ri[(int64_t)c * n + k], s);
-          S[(int64_t)c * n + r] = s;
+          S[(int64_t)c * n + r] = ukg_df::to_f64(s);
         }
       }
       __syncthreads();
@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(NT) solve_cta(CArgs<T> a, int want_cov)
     double* So = a.cov + oj * nn;
     for (int e = tid; e < n * n; e += NT) { /* X now holds S^T = S; column-major out */
       const int r = e / n, c = e - r * n;
-      So[(int64_t)c * n + r] = X[e];
+      So[(int64_t)c * n + r] = ukg_df::to_f64(X[e]);
     }
     __syncthreads();
   }

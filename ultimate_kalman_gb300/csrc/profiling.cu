@@ -36,7 +36,8 @@ const char* kNames[UKG_K_COUNT] = {"weigh_kernel", "pair_kernel", "tail_kernel",
                                    "assoc_element_kernel", "assoc_scan_kernel", "assoc_smooth_kernel",
                                    "refine_kernel", "fp32_pair_kernel", "fp32_solve_kernel",
                                    "refine_residual_kernel", "refine_rt_kernel", "refine_solve_kernel",
-                                   "build_kernel", "filter_kernel"};
+                                   "build_kernel", "filter_kernel", "df_weigh_kernel", "df_pair_kernel",
+                                   "df_tail_kernel", "df_solve_kernel"};
 
 cudaEvent_t get_event()
 {

@@ -20,6 +20,10 @@ enum {
   UKG_K_RSOLVE,
   UKG_K_BUILD,
   UKG_K_FILTER,
+  UKG_K_DF_WEIGH, /* the precision form with covariances: double-float kernels */
+  UKG_K_DF_PAIR,
+  UKG_K_DF_TAIL,
+  UKG_K_DF_SOLVE,
   UKG_K_COUNT
 };
 

@@ -29,6 +29,12 @@ void ukg_release_filter_workspace(void);
 
 /* checks the arguments of a packed problem that do not need device access   */
 int ukg_validate_problem(const kalman_gpu_problem_t* p, int need_cov);
+/* Lets `kernel` launch with up to the device's opt-in maximum of dynamic
+ * shared memory.  The attribute is process-wide, so it is raised once per
+ * (device, kernel) to the maximum rather than set per call: per-call values
+ * raced between host threads smoothing different shapes (one thread lowered
+ * the limit just before another launched a larger request).              */
+void ukg_allow_dynamic_smem(const void* kernel);
 
 #ifdef __cplusplus
 }

@@ -168,8 +168,23 @@ def plan_flops_fast_fp32(track_lengths, n, m0, sweeps=2):
             "fp32_solve_kernel": f["solve_kernel"], "refine_kernel": refine_flops(track_lengths, n, m0, sweeps)}
 
 
+def compulsory_bytes(track_lengths, n, m, covariance=False):
+    """The smoothing problem's compulsory DRAM bytes (FP64): every step's
+    equations read once at their real sizes -- F, H, K (n x n), c (n), G
+    (m x n), o (m), C (m x m) -- and the smoothed state (n), plus its
+    covariance (n x n), written once.  Returns (bytes in, bytes out); for
+    n=6, m=3: 1,152 B in and 48 B (states) or 336 B (with covariances) out per
+    step.  Everything else a kernel moves (padding of the packed layout,
+    weighed equations, level equations, records) is traffic above this."""
+    N = float(np.asarray(track_lengths, dtype=np.int64).sum())
+    per_in = (3 * n * n + n + m * n + m + m * m) * 8
+    per_out = (n + (n * n if covariance else 0)) * 8
+    return N * per_in, N * per_out
+
+
 def plan_bytes_fast(track_lengths, n, m, fp32=False, sweeps=1):
-    """Algorithmic DRAM bytes per kernel category for one states-only smoothing
+    """Modelled DRAM traffic per kernel category (not the algorithmic bytes:
+    those are compulsory_bytes) for one states-only smoothing
     of tracks with n states and m observation rows per step: every input block
     read once, every output and intermediate written once and read once.
 

@@ -100,7 +100,8 @@ EXPORTED = [
     "kalman_gpu_release", "kalman_gpu_profile_enable", "kalman_gpu_profile_read", "kalman_gpu_launch_count",
     "kalman_gpu_measure_fp64_tflops", "kalman_gpu_measure_fp32_tflops", "kalman_gpu_smooth_oddeven_noalloc",
     "kalman_gpu_plan_create", "kalman_gpu_plan_execute", "kalman_gpu_plan_status", "kalman_gpu_plan_destroy",
-    "kalman_gpu_expand_invariant", "kalman_gpu_filter_packed",
+    "kalman_gpu_expand_invariant", "kalman_gpu_filter_packed", "kalman_gpu_oddeven_workspace_bytes",
+    "kalman_gpu_workspace_held",
 ]
 
 _lib = None
@@ -145,6 +146,9 @@ def load(path=LIB_PATH):
     L.kalman_gpu_expand_invariant.argtypes = [P, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(InvariantModel),
                                               ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
     L.kalman_gpu_expand_invariant.restype = ctypes.c_int
+    L.kalman_gpu_oddeven_workspace_bytes.argtypes = [ctypes.c_uint32, P]
+    L.kalman_gpu_oddeven_workspace_bytes.restype = ctypes.c_int64
+    L.kalman_gpu_workspace_held.restype = ctypes.c_int64
     _lib = L
     return L
 
@@ -167,10 +171,10 @@ def profile_enable(on=True):
 def profile_read():
     """{kernel name: (total ms, launches)} since profile_enable()."""
     L = load()
-    names = (ctypes.c_char_p * 16)()
-    ms = (ctypes.c_double * 16)()
-    cnt = (ctypes.c_int64 * 16)()
-    k = L.kalman_gpu_profile_read(16, names, ms, cnt)
+    names = (ctypes.c_char_p * 32)()
+    ms = (ctypes.c_double * 32)()
+    cnt = (ctypes.c_int64 * 32)()
+    k = L.kalman_gpu_profile_read(32, names, ms, cnt)
     return {names[i].decode(): (ms[i], cnt[i]) for i in range(k)}
 
 
@@ -184,6 +188,24 @@ def measure_fp64_tflops(active_lanes=32):
 
 def measure_fp32_tflops():
     return load().kalman_gpu_measure_fp32_tflops()
+
+
+def oddeven_workspace_bytes(s, **kw):
+    """kalman_gpu_oddeven_workspace_bytes for a ProblemStruct and the options
+    that options_for(**kw) gives."""
+    return load().kalman_gpu_oddeven_workspace_bytes(options_for("oddeven", **kw), ctypes.byref(s))
+
+
+def workspace_held():
+    """kalman_gpu_workspace_held: device bytes the calling thread's library
+    state holds."""
+    return load().kalman_gpu_workspace_held()
+
+
+def release():
+    """kalman_gpu_release: frees the library's cached device workspace and
+    staging buffers of the calling thread."""
+    load().kalman_gpu_release()
 
 
 def options_for(algorithm, covariance=True, fp32_refine=False, sweeps=0, tf32x3=False):
