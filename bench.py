@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the library's default tuning")
     ap.add_argument("--no-large", action="store_true", help="skip the n=128 large-state line")
     ap.add_argument("--fp32-only", action="store_true",
                     help="time the precision form only (no plain FP64 pass, probes, e2e or CPU leg): profiling runs")
@@ -188,6 +189,21 @@ def time_smooths(D, steps, stream, **kw):
     return evs[0].elapsed_time(evs[-1]) / steps, per
 
 
+def time_plan(plan, steps, stream):
+    """Times `steps` replays of a plan's CUDA graph, each bracketed by CUDA
+    events on `stream`; returns (mean ms, per-replay ms list)."""
+    import torch
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    torch.cuda.synchronize()
+    evs[0].record(stream)
+    for i in range(steps):
+        plan.execute(stream)
+        evs[i + 1].record(stream)
+    torch.cuda.synchronize()
+    per = [evs[i].elapsed_time(evs[i + 1]) for i in range(steps)]
+    return evs[0].elapsed_time(evs[-1]) / steps, per
+
+
 def roofline_for(prof, fl, steps, fp64_peak, fp32_peak, hbm_peak, compulsory_in, traffic_model):
     """Roofline of the kernel category with the largest time.
 
@@ -256,7 +272,7 @@ def time_call(fn, reps, stream):
 
 def run_gpu(args):
     import torch
-    from ultimate_kalman_gb300 import build, flops, native
+    from ultimate_kalman_gb300 import autotune, build, flops, native
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     if world > 1:
@@ -267,8 +283,24 @@ def run_gpu(args):
     P = workload(args.tracks, rank)
     D = native.DeviceProblem(P, covariance=True)
     fp32 = dict(covariance=False, fp32_refine=True, sweeps=args.sweeps)
+    stream = torch.cuda.current_stream()
+    # the autotuner picks the work mapping and block shapes for this class (about a second here)
+    tuned = autotune.tune(D, fp32_refine=True, covariance=False, sweeps=args.sweeps, reps=3, stream=stream,
+                          save=False) if not args.no_tune else None
+    # kernels and per-kernel times of one smoothing by direct calls (also the warm-up)
     for _ in range(args.warmup):
         D.smooth("oddeven", **fp32)
+    prof_steps = max(3, args.steps // 2)
+    native.profile_enable(True)
+    launches0 = native.launch_count()
+    ms_direct, _ = time_smooths(D, prof_steps, stream, **fp32)
+    launches_per = (native.launch_count() - launches0) / prof_steps
+    prof = native.profile_read()
+    native.profile_enable(False)
+    # the timed steps: the smoothing captured once into a CUDA graph (kalman_gpu_plan_*) and replayed
+    plan = D.plan("oddeven", **fp32)
+    for _ in range(args.warmup):
+        plan.execute(stream)
     torch.cuda.synchronize()
 
     def barrier():
@@ -277,16 +309,14 @@ def run_gpu(args):
 
     sampler = ClockSampler(local)
     time.sleep(0.5)  # let the sampler start before the timed region
-    stream = torch.cuda.current_stream()
-    native.profile_enable(True)
-    launches0 = native.launch_count()
     barrier()
-    ms, per = time_smooths(D, args.steps, stream, **fp32)
+    ms, per = time_plan(plan, args.steps, stream)
     barrier()
-    launches = native.launch_count() - launches0
-    prof = native.profile_read()
-    native.profile_enable(False)
     clocks = sampler.stop()
+    if plan.status() != 0:
+        raise RuntimeError("the plan's smoothing reported %s" % (native.last_error(),))
+    plan.close()
+    launches = int(round(launches_per * args.steps))
     X32 = D.state.clone()
     if world > 1:
         t = torch.tensor([ms], device="cuda")
@@ -303,14 +333,33 @@ def run_gpu(args):
             torch.distributed.destroy_process_group()
         return
 
-    # the plain FP64 path: states + covariances, and states only
-    D.smooth("oddeven", covariance=True)
-    native.profile_enable(True)
-    ms64c, _ = time_smooths(D, max(2, args.steps // 2), stream, covariance=True)
-    prof64 = native.profile_read()
-    native.profile_enable(False)
-    ms64, _ = time_smooths(D, max(2, args.steps // 2), stream, covariance=False)
-    X64 = D.state
+    # the plain FP64 path (states + covariances, and states only) and the precision form with
+    # covariances (double-float), each under its own tuning
+    k2 = max(2, args.steps // 2)
+    tunings = {"fp32_refine_states": tuned}
+    for name, kw in (("fp64_states_and_covariances", dict(covariance=True)),
+                     ("fp64_states", dict(covariance=False)),
+                     ("fp32_refine_states_and_covariances", dict(covariance=True, fp32_refine=True))):
+        tunings[name] = autotune.tune(D, reps=2, stream=stream, save=False, **kw) if not args.no_tune else None
+        D.smooth("oddeven", **kw)
+        if name == "fp64_states_and_covariances":
+            native.profile_enable(True)
+            ms64c, _ = time_smooths(D, k2, stream, **kw)
+            prof64 = native.profile_read()
+            native.profile_enable(False)
+            S64 = D.cov.clone()
+            X64c = D.state.clone()
+        elif name == "fp64_states":
+            ms64, _ = time_smooths(D, k2, stream, **kw)
+        else:
+            native.profile_enable(True)
+            msdd, _ = time_smooths(D, k2, stream, **kw)
+            profdd = native.profile_read()
+            native.profile_enable(False)
+            err_dd = {"states": rel_states(D.state, X64c), "covariances": rel_states(D.cov, S64)}
+            del S64
+    native.set_tuning(default=True)
+    X64 = X64c
     err = float(((X32 - X64).abs().amax(dim=1) / X64.abs().amax(dim=1)).max().item())
 
     peak64 = native.measure_fp64_tflops(32)
@@ -323,13 +372,13 @@ def run_gpu(args):
     by64 = flops.plan_bytes_fast(P.track_lengths(), 6, 3, fp32=False)
     comp = flops.compulsory_bytes(P.track_lengths(), 6, 3, covariance=False)
     comp_cov = flops.compulsory_bytes(P.track_lengths(), 6, 3, covariance=True)
-    roof = roofline_for(prof, fl32, args.steps, peak64, peak32, peaks["hbm_gbs"], comp[0], by32)
+    roof = roofline_for(prof, fl32, prof_steps, peak64, peak32, peaks["hbm_gbs"], comp[0], by32)
     tfile = os.path.join(REPO, "profiles", "traffic_per_launch.json")
     if os.path.exists(tfile):
         roof["traffic"] = json.load(open(tfile)).get(roof["kernel"])
-    roof["per_kernel"] = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps,
+    roof["per_kernel"] = {k: {"ms_per_step": v[0] / prof_steps, "launches_per_step": v[1] / prof_steps,
                               "share": v[0] / sum(x[0] for x in prof.values())} for k, v in prof.items()}
-    roof64 = roofline_for(prof64, fl64, max(2, args.steps // 2), peak64, peak32, peaks["hbm_gbs"], comp_cov[0], by64)
+    roof64 = roofline_for(prof64, fl64, k2, peak64, peak32, peaks["hbm_gbs"], comp_cov[0], by64)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -341,8 +390,17 @@ def run_gpu(args):
             "clocks": clocks,
             "plain_fp64": {"states_and_covariances": total_steps / (ms64c * 1e-3),
                            "states_only": total_steps / (ms64 * 1e-3), "unit": UNIT,
-                           "speedup_fp32_refine_vs_fp64_states_only": ms64 / ms,
-                           "speedup_fp32_refine_vs_fp64_with_covariances": ms64c / ms, "roofline": roof64},
+                           "speedup_fp32_refine_vs_fp64_states_only": ms64 / ms, "roofline": roof64},
+            "precision_form_with_covariances": {
+                "value": total_steps / (msdd * 1e-3), "unit": UNIT, "ms_per_step": msdd,
+                "form": "double-float (FP32 pairs, ~47 bits) factorization and covariance recurrence",
+                "rel_err_vs_fp64": err_dd, "speedup_vs_fp64_states_and_covariances": ms64c / msdd,
+                "per_kernel_ms": {k: v[0] / k2 for k, v in profdd.items()}},
+            "execution": {"timed": "kalman_gpu_plan_execute: the smoothing captured once into a CUDA graph",
+                          "plan_graph_ms": ms, "direct_call_ms": ms_direct,
+                          "kernels_per_smoothing": launches_per},
+            "tuning": {k: ({"tuning": v["tuning"], "ms": v["ms"], "default_ms": v["default_ms"],
+                            "trials": len(v["table"])} if v else None) for k, v in tunings.items()},
             "peaks": {"fp64_tflops": peak64, "fp32_tflops": peak32, "hbm_gbs": peaks["hbm_gbs"]}}
 
     # filtered estimates of the same tracks (the sequential filter, tracks in parallel)

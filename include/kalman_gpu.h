@@ -218,6 +218,32 @@ void kalman_gpu_plan_destroy(kalman_gpu_plan_t* plan);
 int64_t kalman_gpu_oddeven_workspace_bytes(uint32_t options, const kalman_gpu_problem_t* p);
 int64_t kalman_gpu_workspace_held(void);
 
+/* Launch tuning of the odd-even smoother (no reference counterpart; the
+ * reference's only knob is the TBB grain, parallel_set_blocksize).  The
+ * setting is process-wide and applies to calls (and plans) that start after
+ * it; the project's autotuner (ultimate_kalman_gb300/autotune.py) measures
+ * the choices per problem class and records the best.
+ *   cta_min_n    state dimension from which one thread block takes a work
+ *                item (a step pair, a tail, an even step) instead of one
+ *                thread; 1..129 (129: never below 129 states), default 9.
+ *                Shapes with more than 8 observation rows always use blocks.
+ *   ctas_per_sm  thread blocks per SM of the block-per-item kernels'
+ *                persistent grid, 1..16, default 4.
+ *   pair_block   threads per block of the FP32 register-tile pair kernel
+ *                (precision form, n = 4 and 6): 32, 64 or 128, default 64.
+ *   weigh_block  steps per block of the double-float weighing kernel
+ *                (precision form, n = 4 and 6): 64, 128 or 256, default 128.
+ * kalman_gpu_set_tuning(NULL) restores the defaults; values outside these
+ * ranges are refused with KALMAN_GPU_EINVAL (the setting is unchanged).    */
+typedef struct kalman_gpu_tuning_st {
+  int32_t cta_min_n;
+  int32_t ctas_per_sm;
+  int32_t pair_block;
+  int32_t weigh_block;
+} kalman_gpu_tuning_t;
+int  kalman_gpu_set_tuning(const kalman_gpu_tuning_t* t);
+void kalman_gpu_get_tuning(kalman_gpu_tuning_t* t);
+
 /* Releases the device workspace and pinned staging buffers cached by the
  * library for the current device.                                            */
 void kalman_gpu_release(void);

@@ -800,7 +800,7 @@ int ensure(size_t bytes, void** out, cudaStream_t st)
     tl_ws = Workspace();
   }
   if (!tl_ws.dev) {
-    size_t want = bytes + (bytes >> 3);
+    size_t want = ukg_with_slack(bytes);
     if (cudaMallocAsync(&tl_ws.dev, want, st) != cudaSuccess) {
       cudaGetLastError();
       tl_ws = Workspace();

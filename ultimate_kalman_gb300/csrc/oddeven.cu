@@ -693,17 +693,21 @@ struct DfWeights {
   }
 };
 
-template <int N, int MX>
-__global__ void __launch_bounds__(kWeighBS, 4) weigh_df_kernel(Args<float, float> a, Eq<float> lo, RawDev raw,
-                                                            int64_t nsteps, int bulk)
+/* BS: threads (steps) per block, a tuning choice (64, 128 or 256); the
+ * register budget per thread is that of four 128-thread blocks per SM.
+ * (Staging the next part while weighing this one, in two buffers, was slower:
+ * the doubled shared memory halves the resident blocks.)                     */
+template <int N, int MX, int BS = kWeighBS>
+__global__ void __launch_bounds__(BS, 512 / BS) weigh_df_kernel(Args<float, float> a, Eq<float> lo, RawDev raw,
+                                                               int64_t nsteps, int bulk)
 {
   using namespace ukg_df;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   double* buf = reinterpret_cast<double*>(smem_raw + 16);
   const int tid = threadIdx.x;
-  const int64_t g0 = (int64_t)blockIdx.x * kWeighBS, g = g0 + tid;
-  const int cnt = (int)((nsteps - g0) < kWeighBS ? (nsteps - g0) : kWeighBS);
+  const int64_t g0 = (int64_t)blockIdx.x * BS, g = g0 + tid;
+  const int cnt = (int)((nsteps - g0) < BS ? (nsteps - g0) : BS);
   const bool active = tid < cnt;
   const int mm = raw.mmax;
   if (tid == 0) mbar_init(bar);
@@ -747,7 +751,7 @@ __global__ void __launch_bounds__(kWeighBS, 4) weigh_df_kernel(Args<float, float
     }
     if (per == 0) continue;
     const uint32_t bytes = (uint32_t)cnt * per * sizeof(double);
-    if (bulk && bytes % 16 == 0) { /* one bulk copy; both addresses are 16-byte aligned (g0 is a multiple of 128) */
+    if (bulk && bytes % 16 == 0) { /* one bulk copy; both addresses are 16-byte aligned (g0 is a multiple of 64) */
       if (tid == 0) bulk_load(buf, src + g0 * per, bytes, bar);
       const bool ok = mbar_wait(bar, phase);
       if (!__syncthreads_and(ok)) { /* the same decision in every thread */
@@ -757,7 +761,7 @@ __global__ void __launch_bounds__(kWeighBS, 4) weigh_df_kernel(Args<float, float
       }
       phase ^= 1;
     } else {
-      for (int e = tid; e < cnt * per; e += kWeighBS) buf[e] = src[g0 * per + e];
+      for (int e = tid; e < cnt * per; e += BS) buf[e] = src[g0 * per + e];
       __syncthreads();
     }
     if (active) {
@@ -1330,14 +1334,14 @@ __device__ __forceinline__ void ss_dispatch_c(int rc, const PairSlice<N, BP>& S,
   }
 }
 
-constexpr int kPairSsBP = 64;
+constexpr int kPairSsBP = 64; /* default block size; 32 and 128 are tuning choices */
 
-template <int N>
-__global__ void __launch_bounds__(kPairSsBP) pair_ss_kernel(Args<float, float> a, int)
+template <int N, int BP = kPairSsBP>
+__global__ void __launch_bounds__(BP) pair_ss_kernel(Args<float, float> a, int)
 {
-  using L = PairSlice<N, kPairSsBP>;
+  using L = PairSlice<N, BP>;
   extern __shared__ __align__(16) float ss_smem[];
-  const int64_t item = (int64_t)blockIdx.x * kPairSsBP + threadIdx.x;
+  const int64_t item = (int64_t)blockIdx.x * BP + threadIdx.x;
   if (item >= a.ct.npairs) return;
   const int t = find_track(a.ct.pair, a.ntracks, item);
   const int64_t p = item - a.ct.pair[t];
@@ -1387,9 +1391,9 @@ __global__ void __launch_bounds__(kPairSsBP) pair_ss_kernel(Args<float, float> a
   }
   cp_async_commit();
 
-  ss_dispatch_a<N, kPairSsBP>(mj + N, S);
+  ss_dispatch_a<N, BP>(mj + N, S);
   if (mj + mj1 == 0) a.ne.m[sn] = 0;
-  else ss_dispatch_c<N, kPairSsBP>(mj + mj1, S, a.ne, sn, mj);
+  else ss_dispatch_c<N, BP>(mj + mj1, S, a.ne, sn, mj);
   if (p == 0) { /* no stage B: the record is stage A's */
     cp_async_wait<0>();
 #pragma unroll
@@ -1402,7 +1406,7 @@ __global__ void __launch_bounds__(kPairSsBP) pair_ss_kernel(Args<float, float> a
     for (int i = 0; i < N; ++i) a.cr.rhs.at(i, se) = S[L::rt + i];
     return;
   }
-  ss_stage_b<N, kPairSsBP>(S, a.ne, a.cr, sn, se);
+  ss_stage_b<N, BP>(S, a.ne, a.cr, sn, se);
 }
 
 /* ---------------------------------------------------------------------------
@@ -2289,19 +2293,38 @@ constexpr int kResidBS = 128;
 struct DfKernels {
   void (*weigh)(Args<float, float>, Eq<float>, RawDev, int64_t, int) = nullptr;
   void (*resid)(Args<float, float>, Eq<float>, Soa<float>, int64_t) = nullptr;
+  int weigh_bs = kWeighBS;
 };
-DfKernels df_kernels(int n, int mmax)
+DfKernels df_kernels(int n, int mmax, int weigh_bs = kWeighBS)
 {
   DfKernels k;
   const int mx = mmax > n ? mmax : n;
-  if (n == 6 && mx == 6) k.weigh = weigh_df_kernel<6, 6>;
-  if (n == 4 && mx == 4) k.weigh = weigh_df_kernel<4, 4>;
+  k.weigh_bs = weigh_bs;
+#define UKG_DFW(N_)                                                                                                 \
+  if (n == N_ && mx == N_)                                                                                          \
+    k.weigh = weigh_bs == 64 ? weigh_df_kernel<N_, N_, 64>                                                          \
+              : weigh_bs == 256 ? weigh_df_kernel<N_, N_, 256> : weigh_df_kernel<N_, N_, 128>;
+  UKG_DFW(6) UKG_DFW(4)
+#undef UKG_DFW
 #define UKG_DF(N_, M_)                                                                                              \
   if (n == N_ && mmax == M_) k.resid = residual_df_kernel<N_, M_, kResidBS>;
   UKG_DF(6, 6) UKG_DF(6, 3) UKG_DF(6, 2) UKG_DF(4, 4) UKG_DF(4, 2)
 #undef UKG_DF
   if (!k.weigh || !k.resid) k = DfKernels(); /* both or neither */
   return k;
+}
+
+/* Launch tuning (kalman_gpu_set_tuning): process-wide, read once at the
+ * start of every call.  Defaults: a thread per item below 9 states, a thread
+ * block per item from 9 on; four CTAs per SM; the block sizes the FP32
+ * kernels were written for.                                                  */
+kalman_gpu_tuning_t default_tuning() { return kalman_gpu_tuning_t{9, 4, kPairSsBP, kWeighBS}; }
+std::mutex g_tune_mu;
+kalman_gpu_tuning_t g_tune = default_tuning();
+kalman_gpu_tuning_t tuning_now()
+{
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  return g_tune;
 }
 
 struct LevelPlan {
@@ -2333,7 +2356,7 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
  * NULL the tables are written into it (tab_cap entries).  Returns the number
  * of table entries needed, or 0 if the recursion is deeper than kMaxLevels. */
 size_t build_plan(const kalman_gpu_problem_t* p, bool want_cov, bool fp32, bool refine, Plan& P, int64_t* tab,
-                  size_t tab_cap)
+                  size_t tab_cap, bool cta)
 {
   const int n = p->n, T = p->ntracks;
   const int mx = p->mmax > n ? p->mmax : n;
@@ -2409,7 +2432,10 @@ size_t build_plan(const kalman_gpu_problem_t* p, bool want_cov, bool fp32, bool 
     P.o_baseR = take((size_t)std::max(T, 1) * nn * sizeof(float));
     P.o_tmp = take((size_t)std::max(T, 1) * n * sizeof(float));
     P.o_dx = take((size_t)std::max<int64_t>(p->nsteps, 1) * n * sizeof(double));
-    if (df_kernels(n, p->mmax).resid) { /* low parts of the double-float level-0 equations */
+    /* the per-thread path refines with the double-float residual where it is
+       compiled (low parts of the level-0 equations); the CTA path, and the
+       per-thread path elsewhere, with the FP64 residual (its two arrays) */
+    if (!cta && df_kernels(n, p->mmax).resid) {
       P.o_eq0lo = take((size_t)P.S0 * eqd * sizeof(float));
     } else { /* the FP64 residual's intermediate arrays */
       P.o_rE = take((size_t)P.S0 * n * sizeof(double));
@@ -2463,17 +2489,19 @@ struct Kernels {
 };
 
 template <typename T>
-Kernels<T> choose_kernels(int n, int mx)
+Kernels<T> choose_kernels(int n, int mx, int pair_bp = kPairSsBP)
 {
   Kernels<T> k;
   if constexpr (sizeof(T) == sizeof(float)) {
     if (n == mx && (n == 6 || n == 4)) {
-      k.pair = n == 6 ? pair_ss_kernel<6> : pair_ss_kernel<4>;
+      if (n == 6)
+        k.pair = pair_bp == 32 ? pair_ss_kernel<6, 32> : pair_bp == 128 ? pair_ss_kernel<6, 128> : pair_ss_kernel<6, 64>;
+      else
+        k.pair = pair_bp == 32 ? pair_ss_kernel<4, 32> : pair_bp == 128 ? pair_ss_kernel<4, 128> : pair_ss_kernel<4, 64>;
       k.solve = n == 6 ? solve_kernel<T, 6, 64> : solve_kernel<T, 4, 64>;
-      k.bp = kPairSsBP;
+      k.bp = pair_bp;
       k.bs = 64;
-      k.pair_smem = (size_t)kPairSsBP * sizeof(float) *
-                    (n == 6 ? PairSlice<6, kPairSsBP>::width : PairSlice<4, kPairSsBP>::width);
+      k.pair_smem = (size_t)pair_bp * sizeof(float) * (n == 6 ? PairSlice<6, 64>::width : PairSlice<4, 64>::width);
       return k;
     }
   }
@@ -2590,7 +2618,8 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
       pick_block(pt_solve, 64, &bs) || pick_block(pt_res, 128, &br))
     return ukg_set_error(KALMAN_GPU_EINVAL, "state dimension %d (observation rows %d) needs more shared memory per "
                          "thread than this build's odd-even kernels use", n, mx);
-  const Kernels<T> K = choose_kernels<T>(n, mx);
+  const kalman_gpu_tuning_t tune = tuning_now();
+  const Kernels<T> K = choose_kernels<T>(n, mx, tune.pair_block);
   if (K.bp) bp = K.bp;
   if (K.bs) bs = K.bs;
   ukg_allow_dynamic_smem((const void*)weigh_kernel<T>);
@@ -2611,9 +2640,11 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
 
   /* double-float level-0 weighing and refinement residual where compiled */
   DfKernels DK;
-  if constexpr (sizeof(T) == sizeof(float)) DK = df_kernels(n, p->mmax);
+  if constexpr (sizeof(T) == sizeof(float)) DK = df_kernels(n, p->mmax, tune.weigh_block);
   const bool use_df = DK.resid != nullptr && P.refine && P.o_eq0lo != 0;
   if (!use_df) DK = DfKernels();
+  if (P.refine && !use_df && (P.o_rE == 0 || P.o_rO == 0)) /* offset 0 is the tables: never write there */
+    return ukg_set_error(KALMAN_GPU_EINVAL, "internal: the workspace has no FP64 residual arrays");
   Eq<float> eq0lo;
   memset(&eq0lo, 0, sizeof(eq0lo));
   RegSolves RS; /* register-resident FP32 solves where compiled */
@@ -2634,12 +2665,13 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
     w.flag = dflag;
     bool done = false;
     if constexpr (sizeof(T) == sizeof(float)) {
-      const size_t smem_df = 16 + (size_t)kWeighBS * blk * sizeof(double);
+      const int wbs = DK.weigh_bs;
+      const size_t smem_df = 16 + (size_t)wbs * blk * sizeof(double);
       if (DK.weigh && smem_df <= (size_t)optin) {
         ukg_allow_dynamic_smem((const void*)DK.weigh);
         UKG_LAUNCH(UKG_K_WEIGH, st,
-                   (DK.weigh<<<grid(p->nsteps, kWeighBS), kWeighBS, smem_df, st>>>(w, eq0lo, raw, p->nsteps,
-                                                                                    (align_bits & 15) == 0)));
+                   (DK.weigh<<<grid(p->nsteps, wbs), wbs, smem_df, st>>>(w, eq0lo, raw, p->nsteps,
+                                                                          (align_bits & 15) == 0)));
         done = true;
       }
     }
@@ -2839,7 +2871,7 @@ int ensure_workspace(size_t bytes, void** out, cudaStream_t st)
     w.dev_bytes = 0;
   }
   if (!w.dev) {
-    size_t want = bytes + (bytes >> 3);
+    size_t want = ukg_with_slack(bytes);
     cudaError_t e = cudaMallocAsync(&w.dev, want, st);
     if (e != cudaSuccess) {
       cudaGetLastError();
@@ -2868,7 +2900,6 @@ extern "C" void ukg_release_oddeven_workspace(void)
 /* ---------------------------------------------------------------------------
  * larger state dimensions: one CTA per item (oddeven_cta.cuh), FP64
  * ------------------------------------------------------------------------ */
-constexpr int kCtaMinN = 9; /* per-thread kernels below, CTA kernels from here on */
 constexpr int kCtaMaxN = 128;
 static_assert(kCtaMaxN <= 32 * ctak::kRtQ && kCtaMaxN <= cta::kMaxCov && 2 * kCtaMaxN <= cta::kMaxPanelRows,
               "CTA kernels: per-lane state registers, covariance and panel buffers");
@@ -2884,12 +2915,21 @@ int64_t cta_scratch_per_cta(int n, int mmax)
   return std::max(std::max(weigh, tail), std::max(pair, solve)) + 32;
 }
 
-int cta_count()
+/* thread blocks of the CTA kernels' persistent grid: per_sm on every SM */
+int cta_count(int per_sm)
 {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  return std::max(sms, 1) * 4;
+  return std::max(sms, 1) * std::max(per_sm, 1);
+}
+
+/* thread per item below tune.cta_min_n states (and up to 8 observation
+ * rows), one thread block per item from there on                           */
+bool use_cta(const kalman_gpu_problem_t* p, const kalman_gpu_tuning_t& tune)
+{
+  const int mxp = p->mmax > p->n ? p->mmax : p->n;
+  return p->n >= tune.cta_min_n || mxp > 8;
 }
 
 template <typename T>
@@ -2904,6 +2944,8 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
   const LevelPlan* lp = P.lp;
   int64_t* dtab = (int64_t*)(B + P.o_tab);
   int* dflag = (int*)(B + P.o_flag);
+  if (P.refine && (P.o_rE == 0 || P.o_rO == 0)) /* offset 0 is the tables: never write there */
+    return ukg_set_error(KALMAN_GPU_EINVAL, "internal: the workspace has no FP64 residual arrays");
   if (tab_dev) /* null: the tables are already in the workspace */
     upload_tables_kernel<<<(unsigned)std::min<size_t>((P.tab_entries + 255) / 256, 1024), 256, 0, st>>>(
         dtab, tab_dev, (int64_t)P.tab_entries);
@@ -3119,18 +3161,19 @@ extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* 
   if (p->nsteps == 0) return 0;
   const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
   const int mxp = p->mmax > p->n ? p->mmax : p->n;
-  if (p->n >= kCtaMinN || mxp > 8) { /* larger shapes: CTA kernels (FP64, or FP32 + refinement) */
+  const kalman_gpu_tuning_t tune = tuning_now();
+  if (use_cta(p, tune)) { /* larger shapes: CTA kernels (FP64, or FP32 + refinement) */
     if (mxp > kCtaMaxN)
       return ukg_set_error(KALMAN_GPU_EINVAL, "state dimension %d (observation rows %d) above this build's limit %d",
                            p->n, p->mmax, kCtaMaxN);
     const bool dd = (options & KALMAN_GPU_FP32_REFINE) && want_cov; /* double-float with covariances */
     const bool f32 = (options & KALMAN_GPU_FP32_REFINE) && !dd;
     Plan P;
-    const size_t need = build_plan(p, want_cov, f32, f32, P, nullptr, 0);
+    const size_t need = build_plan(p, want_cov, f32, f32, P, nullptr, 0, true);
     if (need == 0) return ukg_set_error(KALMAN_GPU_EINVAL, "tracks longer than 2^%d steps", kMaxLevels - 1);
     if (int e = ensure_mapped_tables(need)) return e;
-    build_plan(p, want_cov, f32, f32, P, tl_mtab.host, need);
-    const int ncta = cta_count();
+    build_plan(p, want_cov, f32, f32, P, tl_mtab.host, need, true);
+    const int ncta = cta_count(tune.ctas_per_sm);
     const int64_t per = cta_scratch_per_cta(p->n, p->mmax);
     const size_t scratch_off = align_up(P.bytes, 256);
     void* base = nullptr;
@@ -3148,11 +3191,11 @@ extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* 
   const bool dd = (options & KALMAN_GPU_FP32_REFINE) && want_cov; /* double-float with covariances */
   const bool fp32 = (options & KALMAN_GPU_FP32_REFINE) && !dd;
   Plan P;
-  const size_t need = build_plan(p, want_cov, fp32, fp32, P, nullptr, 0);
+  const size_t need = build_plan(p, want_cov, fp32, fp32, P, nullptr, 0, false);
   if (need == 0) return ukg_set_error(KALMAN_GPU_EINVAL, "tracks longer than 2^%d steps", kMaxLevels - 1);
   if (int e = ensure_mapped_tables(need)) return e;
   int64_t* tab = tl_mtab.host;
-  build_plan(p, want_cov, fp32, fp32, P, tab, need);
+  build_plan(p, want_cov, fp32, fp32, P, tab, need, false);
   void* base = nullptr;
   if (int e = ensure_workspace(P.bytes, &base, (cudaStream_t)cuda_stream)) return e;
   if (fp32) return run_plan<float>(options, p, (cudaStream_t)cuda_stream, P, tab, (char*)base, tl_mtab.dev);
@@ -3173,14 +3216,39 @@ extern "C" int64_t kalman_gpu_oddeven_workspace_bytes(uint32_t options, const ka
   const bool f32 = (options & KALMAN_GPU_FP32_REFINE) && !want_cov; /* with covariances: double-float, 8 bytes */
   const int mxp = p->mmax > p->n ? p->mmax : p->n;
   Plan P;
-  if (build_plan(p, want_cov, f32, f32, P, nullptr, 0) == 0) {
+  const kalman_gpu_tuning_t tune = tuning_now();
+  const bool cta = use_cta(p, tune);
+  if (build_plan(p, want_cov, f32, f32, P, nullptr, 0, cta) == 0) {
     ukg_set_error(KALMAN_GPU_EINVAL, "tracks longer than 2^%d steps", kMaxLevels - 1);
     return -1;
   }
   size_t bytes = P.bytes;
-  if (p->n >= kCtaMinN || mxp > 8)
-    bytes = align_up(P.bytes, 256) + (size_t)cta_count() * cta_scratch_per_cta(p->n, p->mmax) * sizeof(double);
-  return (int64_t)(bytes + (bytes >> 3));
+  if (cta)
+    bytes = align_up(P.bytes, 256) +
+            (size_t)cta_count(tune.ctas_per_sm) * cta_scratch_per_cta(p->n, p->mmax) * sizeof(double);
+  return (int64_t)ukg_with_slack(bytes);
+}
+
+extern "C" int kalman_gpu_set_tuning(const kalman_gpu_tuning_t* t)
+{
+  ukg_clear_error();
+  kalman_gpu_tuning_t v = t ? *t : default_tuning();
+  if (v.cta_min_n < 1 || v.cta_min_n > kCtaMaxN + 1)
+    return ukg_set_error(KALMAN_GPU_EINVAL, "cta_min_n %d outside 1..%d", v.cta_min_n, kCtaMaxN + 1);
+  if (v.ctas_per_sm < 1 || v.ctas_per_sm > 16)
+    return ukg_set_error(KALMAN_GPU_EINVAL, "ctas_per_sm %d outside 1..16", v.ctas_per_sm);
+  if (v.pair_block != 32 && v.pair_block != 64 && v.pair_block != 128)
+    return ukg_set_error(KALMAN_GPU_EINVAL, "pair_block %d is not 32, 64 or 128", v.pair_block);
+  if (v.weigh_block != 64 && v.weigh_block != 128 && v.weigh_block != 256)
+    return ukg_set_error(KALMAN_GPU_EINVAL, "weigh_block %d is not 64, 128 or 256", v.weigh_block);
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune = v;
+  return 0;
+}
+
+extern "C" void kalman_gpu_get_tuning(kalman_gpu_tuning_t* t)
+{
+  if (t) *t = tuning_now();
 }
 
 /* ---------------------------------------------------------------------------
@@ -3248,11 +3316,11 @@ extern "C" int kalman_gpu_smooth_oddeven_noalloc(uint32_t options, const kalman_
   }
   const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
   Plan P;
-  const size_t need = build_plan(p, want_cov, false, false, P, nullptr, 0);
+  const size_t need = build_plan(p, want_cov, false, false, P, nullptr, 0, false);
   if (need == 0 || need > kNoallocTabEntries)
     return ukg_set_error(KALMAN_GPU_EINVAL, "the allocation-free entry point plans at most %zu table entries "
                          "(this problem needs %zu: too many tracks)", kNoallocTabEntries, need);
-  build_plan(p, want_cov, false, false, P, g_noalloc_tab, kNoallocTabEntries);
+  build_plan(p, want_cov, false, false, P, g_noalloc_tab, kNoallocTabEntries, false);
   if (P.bytes > (size_t)KALMAN_GPU_NOALLOC_SCRATCH_BYTES)
     return ukg_set_error(KALMAN_GPU_EINVAL, "this problem needs %zu bytes of scratch; the allocation-free entry "
                          "point has %zu (use kalman_gpu_smooth_oddeven_packed)", P.bytes,
@@ -3321,7 +3389,8 @@ extern "C" kalman_gpu_plan_t* kalman_gpu_plan_create(uint32_t options, const kal
   }
   const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
   const int mxp = p->mmax > p->n ? p->mmax : p->n;
-  const bool cta = p->n >= kCtaMinN || mxp > 8;
+  const kalman_gpu_tuning_t tune = tuning_now();
+  const bool cta = use_cta(p, tune);
   if (cta && mxp > kCtaMaxN) {
     ukg_set_error(KALMAN_GPU_EINVAL, "state dimension %d (observation rows %d) above this build's limit %d", p->n,
                   p->mmax, kCtaMaxN);
@@ -3330,17 +3399,17 @@ extern "C" kalman_gpu_plan_t* kalman_gpu_plan_create(uint32_t options, const kal
   const bool dd = (options & KALMAN_GPU_FP32_REFINE) && want_cov; /* double-float with covariances */
   const bool fp32 = (options & KALMAN_GPU_FP32_REFINE) && !dd;
   Plan P;
-  const size_t need = build_plan(p, want_cov, fp32, fp32, P, nullptr, 0);
+  const size_t need = build_plan(p, want_cov, fp32, fp32, P, nullptr, 0, cta);
   if (need == 0) {
     ukg_set_error(KALMAN_GPU_EINVAL, "tracks longer than 2^%d steps", kMaxLevels - 1);
     return nullptr;
   }
   std::vector<int64_t> tab(need);
-  build_plan(p, want_cov, fp32, fp32, P, tab.data(), need);
+  build_plan(p, want_cov, fp32, fp32, P, tab.data(), need, cta);
   kalman_gpu_plan* pl = new kalman_gpu_plan();
   pl->cta = cta;
   cudaGetDevice(&pl->device);
-  const int ncta = cta ? cta_count() : 0;
+  const int ncta = cta ? cta_count(tune.ctas_per_sm) : 0;
   const int64_t per = cta ? cta_scratch_per_cta(p->n, p->mmax) : 0;
   const size_t scratch_off = align_up(P.bytes, 256);
   const size_t bytes = cta ? scratch_off + (size_t)ncta * per * sizeof(double) : P.bytes;

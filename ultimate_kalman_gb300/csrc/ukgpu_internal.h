@@ -35,6 +35,14 @@ int ukg_validate_problem(const kalman_gpu_problem_t* p, int need_cov);
  * raced between host threads smoothing different shapes (one thread lowered
  * the limit just before another launched a larger request).              */
 void ukg_allow_dynamic_smem(const void* kernel);
+/* Workspace bytes to allocate for a problem needing `bytes`: 1/8 more, so a
+ * slightly larger next problem reuses it, but at most 1 GiB more (a 150 GB
+ * workspace must not hold 19 GB it will never use).                          */
+static inline size_t ukg_with_slack(size_t bytes)
+{
+  const size_t extra = bytes >> 3;
+  return bytes + (extra < ((size_t)1 << 30) ? extra : ((size_t)1 << 30));
+}
 
 #ifdef __cplusplus
 }

@@ -69,6 +69,15 @@ class ProblemStruct(ctypes.Structure):
     ]
 
 
+class Tuning(ctypes.Structure):
+    """kalman_gpu_tuning_t (include/kalman_gpu.h)."""
+    _fields_ = [("cta_min_n", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("pair_block", ctypes.c_int32),
+                ("weigh_block", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class InvariantModel(ctypes.Structure):
     """kalman_gpu_invariant_model_t (include/kalman_gpu.h): device pointers to
     column-major model matrices."""
@@ -101,7 +110,7 @@ EXPORTED = [
     "kalman_gpu_measure_fp64_tflops", "kalman_gpu_measure_fp32_tflops", "kalman_gpu_smooth_oddeven_noalloc",
     "kalman_gpu_plan_create", "kalman_gpu_plan_execute", "kalman_gpu_plan_status", "kalman_gpu_plan_destroy",
     "kalman_gpu_expand_invariant", "kalman_gpu_filter_packed", "kalman_gpu_oddeven_workspace_bytes",
-    "kalman_gpu_workspace_held",
+    "kalman_gpu_workspace_held", "kalman_gpu_set_tuning", "kalman_gpu_get_tuning",
 ]
 
 _lib = None
@@ -149,6 +158,9 @@ def load(path=LIB_PATH):
     L.kalman_gpu_oddeven_workspace_bytes.argtypes = [ctypes.c_uint32, P]
     L.kalman_gpu_oddeven_workspace_bytes.restype = ctypes.c_int64
     L.kalman_gpu_workspace_held.restype = ctypes.c_int64
+    L.kalman_gpu_set_tuning.argtypes = [ctypes.POINTER(Tuning)]
+    L.kalman_gpu_set_tuning.restype = ctypes.c_int
+    L.kalman_gpu_get_tuning.argtypes = [ctypes.POINTER(Tuning)]
     _lib = L
     return L
 
@@ -200,6 +212,30 @@ def workspace_held():
     """kalman_gpu_workspace_held: device bytes the calling thread's library
     state holds."""
     return load().kalman_gpu_workspace_held()
+
+
+def set_tuning(**knobs):
+    """kalman_gpu_set_tuning with the current values overridden by `knobs`
+    (cta_min_n, ctas_per_sm, pair_block, weigh_block); set_tuning(default=True)
+    restores the library's defaults.  Returns the setting now in force."""
+    L = load()
+    if knobs.pop("default", False):
+        _check(L.kalman_gpu_set_tuning(None))
+    t = get_tuning()
+    for k, v in knobs.items():
+        if k not in t:
+            raise KeyError(k)
+        t[k] = int(v)
+    if knobs:
+        _check(L.kalman_gpu_set_tuning(ctypes.byref(Tuning(**t))))
+    return get_tuning()
+
+
+def get_tuning():
+    """kalman_gpu_get_tuning as a dict."""
+    t = Tuning()
+    load().kalman_gpu_get_tuning(ctypes.byref(t))
+    return t.as_dict()
 
 
 def release():
