@@ -411,8 +411,9 @@ def run_gpu(args):
     if not args.no_e2e:
         del D
         torch.cuda.empty_cache()
-        pin = {f: torch.from_numpy(np.ascontiguousarray(getattr(P, f))).pin_memory() for f in native._FIELDS}
-        st_h = torch.empty((P.nsteps, 6), dtype=torch.float64).pin_memory()
+        (pin, st_h), pin_node = numa_local(lambda: (
+            {f: torch.from_numpy(np.ascontiguousarray(getattr(P, f))).pin_memory() for f in native._FIELDS},
+            torch.empty((P.nsteps, 6), dtype=torch.float64).pin_memory()))
         s = native.host_struct_from_tensors(P, pin, st_h, None)
         native.smooth_struct("oddeven", s, **fp32)  # warm-up (device staging allocated)
         times = []
@@ -428,7 +429,11 @@ def run_gpu(args):
                        "d2h_bytes_per_step": int(st_h.numel() * 8), "ms_per_step": e2e_ms,
                        "path": "kalman_gpu_smooth_oddeven_packed, KALMAN_GPU_HOST arrays, FP32 + refinement",
                        "host_link": link, "h2d_share_at_probe_bandwidth": h2d / (link["h2d_gbs"] * 1e9) / (e2e_ms * 1e-3),
+                       "pinned_buffers_numa_node": pin_node,
                        "all_times_ms": [1e3 * t for t in times]}
+        del pin, st_h, s
+        if rank == 0 and world == 1:
+            line["e2e"]["reference_api"] = secondary(lambda: struct_e2e(P, X32, fp32, args.e2e_steps))
 
     if rank == 0 and world == 1 and not args.no_cpu:
         v, nsteps, ntr, nt, dt, Xo = cpu_sample(P, args.cpu_seconds)
@@ -439,8 +444,6 @@ def run_gpu(args):
                                           f"oracle/kalman_oracle.c odd-even, FP64, states only, OpenMP over tracks",
                                 "rel_err_of_gpu_states_on_sample": err_o}
     if rank == 0 and world == 1 and not args.no_large:
-        if not args.no_e2e:
-            del pin, st_h, s
         torch.cuda.empty_cache()
         for key, fn in (("large_state", lambda: large_state(stream)), ("builder", builder_line),
                         ("config0", lambda: config0_line(stream, not args.no_cpu)),
@@ -451,6 +454,37 @@ def run_gpu(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def struct_e2e(P, X32, kw, reps):
+    """End to end through the reference's own calling convention: one
+    kalman_step_equations_t per step, its matrices pointing at the caller's
+    host data, smoothed by the batched form of kalman_smooth_oddeven
+    (kalman_gpu_smooth_tracks): the library packs the structs into page-locked
+    staging, copies, smooths, copies back and gives every step its own state
+    matrix (the reference's result contract).  Host wall clock per call."""
+    from ultimate_kalman_gb300 import native
+    t0 = time.perf_counter()
+    V = native.EquationsView(P)
+    build_s = time.perf_counter() - t0
+    st = V.smooth_tracks("oddeven", **kw)  # warm-up: page-locked staging allocated
+    if st != 0:
+        raise RuntimeError(str(native.last_error()))
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        st = V.smooth_tracks("oddeven", **kw)
+        times.append(time.perf_counter() - t0)
+        if st != 0:
+            raise RuntimeError(str(native.last_error()))
+    ms = 1e3 * float(np.median(times))
+    sample = np.linspace(0, P.nsteps - 1, 2000).astype(np.int64)
+    err = rel_states(V.states(sample), X32[sample].cpu().numpy())
+    native.release()  # the page-locked staging of this thread
+    return {"value": P.nsteps / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "all_times_ms": [1e3 * t for t in times],
+            "path": "kalman_gpu_smooth_tracks on one kalman_step_equations_t per step (host matrices, results "
+                    "returned as one state matrix per step), FP32 + refinement",
+            "structs_built_s": build_s, "rel_err_vs_device_path_on_2000_steps": err}
 
 
 def filter_line(D, P, stream):
@@ -538,13 +572,51 @@ def secondary(fn):
         return {"error": f"{type(e).__name__}: {e}"}
 
 
+def gpu_numa_cpus():
+    """(NUMA node of the current GPU, the host CPUs of that node) from sysfs,
+    or (None, None)."""
+    import torch
+    try:
+        pr = torch.cuda.get_device_properties(torch.cuda.current_device())
+        bus = f"{pr.pci_domain_id:04x}:{pr.pci_bus_id:02x}:{pr.pci_device_id:02x}.0"
+        with open(f"/sys/bus/pci/devices/{bus}/numa_node") as f:
+            node = int(f.read().strip())
+        if node < 0:
+            return None, None
+        cpus = set()
+        with open(f"/sys/devices/system/node/node{node}/cpulist") as f:
+            for part in f.read().strip().split(","):
+                a, _, b = part.partition("-")
+                cpus.update(range(int(a), int(b or a) + 1))
+        return node, cpus
+    except Exception:
+        return None, None
+
+
+def numa_local(fn):
+    """Runs fn() with this thread restricted to the host CPUs of the GPU's
+    NUMA node (when that is known and allowed), so that page-locked buffers
+    fn allocates are placed in memory local to the GPU's host link; restores
+    the affinity afterwards.  Returns (fn(), node used or None)."""
+    node, cpus = gpu_numa_cpus()
+    old = os.sched_getaffinity(0)
+    use = (old & cpus) if cpus else set()
+    if not use:
+        return fn(), None
+    os.sched_setaffinity(0, use)
+    try:
+        return fn(), node
+    finally:
+        os.sched_setaffinity(0, old)
+
+
 def h2d_probe(gb=4.0):
     """Host-to-device bandwidth of this machine: one copy of a `gb` GB page-locked
     buffer into device memory (cudaMemcpyAsync), CUDA events, best of 3; and
     the host NUMA node of the GPU where sysfs says."""
     import torch
     n = int(gb * 1e9) // 8
-    h = torch.empty(n, dtype=torch.float64).pin_memory()
+    h, _ = numa_local(lambda: torch.empty(n, dtype=torch.float64).pin_memory())
     d = torch.empty(n, dtype=torch.float64, device="cuda")
     best = None
     for _ in range(3):

@@ -9,7 +9,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from ultimate_kalman_gb300 import build, native
+from ultimate_kalman_gb300 import build, native, problem as pb
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -187,3 +187,36 @@ def test_builder_and_filter_refuse_bad_arguments_without_touching_a_device(lib):
     assert lib.kalman_gpu_expand_invariant(ctypes.byref(s), 0, 5, ctypes.byref(bad), None, 3, None, None) == \
         native.KALMAN_GPU_EINVAL
     assert "covariance types" in native.last_error()[1]
+
+
+def test_bulk_equation_structs_equal_the_per_step_builder():
+    """native.EquationsView (numpy-built kalman_step_equations_t arrays that
+    point into the packed arrays) describes exactly the matrices that the
+    per-step ctypes builder copies out: shapes, leading dimensions, values,
+    missing observations and 'w' covariances."""
+    import ctypes
+    P = pb.random_dynamics([40, 3, 17], 4, 3, seed=3, missing=0.2, K_type="w", C_type="w")
+    V = native.EquationsView(P)
+    _, _, structs = native.build_equations(P)
+
+    def mat(p):
+        if not p:
+            return None
+        M = p.contents
+        a = np.ctypeslib.as_array(M.elements, shape=(M.col_dim * M.ld,)).reshape(M.col_dim, M.ld)
+        return a[:, :M.row_dim].T.copy()
+
+    for s in range(P.nsteps):
+        ev = native.StepEquations.from_address(int(V.ptrs[s]))
+        e = structs[s]
+        assert ev.dimension == e.dimension == P.n
+        for f in ("H", "F", "K", "c", "G", "o", "C"):
+            a, b = mat(getattr(ev, f)), mat(getattr(e, f))
+            assert (a is None) == (b is None), (s, f)
+            if a is not None:
+                np.testing.assert_array_equal(a, b)
+        if e.K:
+            assert ev.K_type == e.K_type
+        if e.o:
+            assert ev.C_type == e.C_type
+    assert ctypes.sizeof(native.StepEquations) == V.eq.dtype.itemsize

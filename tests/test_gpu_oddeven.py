@@ -203,3 +203,17 @@ def test_concurrent_host_threads_with_different_shapes():
     for n, (X, S) in results.items():
         np.testing.assert_array_equal(X, alone[n][0])
         np.testing.assert_array_equal(S, alone[n][1])
+
+
+def test_bulk_structs_through_the_batched_reference_entry_equal_the_packed_path():
+    """kalman_gpu_smooth_tracks on numpy-built step structs (the bench's
+    struct-API end-to-end leg) gives the packed entry point's states bit for
+    bit, FP64 and precision form, on repeated calls (each frees the previous
+    call's result matrices)."""
+    P = pb.random_dynamics([700, 3, 129, 1], 5, 3, seed=31, missing=0.1, K_type="w", C_type="F")
+    V = native.EquationsView(P)
+    for f32 in (False, True):
+        Xp, _ = native.smooth(P, "oddeven", covariance=False, fp32_refine=f32)
+        for _ in range(2):
+            assert V.smooth_tracks("oddeven", fp32_refine=f32) == 0, native.last_error()
+            np.testing.assert_array_equal(V.states(np.arange(P.nsteps)), Xp)

@@ -30,14 +30,23 @@ class FakeExecutor:
     def __init__(self, clock, rate=1e6, lanes=1):
         self.clock, self.rate, self.lanes = clock, rate, lanes
         self.resident = set()
+        self.tracks = {}   # track id -> steps kept resident
         self.batches = []
         self.running = []  # (start, finish) of every batch
+
+    def resident_steps(self, tid):
+        return self.tracks.get(tid, 0)
 
     def upload(self, r):
         self.resident.add(r.rid)
 
     def release(self, r):
         self.resident.discard(r.rid)
+        if r.track_id is not None:
+            if r.keep:
+                self.tracks[r.track_id] = r.steps
+            else:
+                self.tracks.pop(r.track_id, None)
 
     def launch(self, batch, lane):
         assert all(r.rid in self.resident for r in batch)
@@ -254,3 +263,58 @@ def test_compact_requests_served_equal_packed_alone():
     for r in done:
         X, _ = native.smooth(r.problem.to_packed(), covariance=False)
         np.testing.assert_array_equal(r.state, X)
+
+
+def test_resident_tracks_are_extended_in_order_and_accounted():
+    """Requests of one track are admitted one at a time, each extending the
+    steps kept from the last; HBM held afterwards is exactly the kept tracks'
+    equations."""
+    clock = Clock()
+    rng = np.random.default_rng(8)
+    full = serve.serving_track(900, 4, 2, rng)
+    pieces = [full.step_range(0, 300), full.step_range(300, 700), full.step_range(700, 900)]
+    reqs = [serve.Request(i, 0.001 * i, P, track_id="t", keep=(i < 2)) for i, P in enumerate(pieces)]
+    other = make_stream(nreq=10, rate=5000.0, seed=9)
+    for j, r in enumerate(other):
+        r.rid = 100 + j
+    ex = FakeExecutor(clock, rate=1e5, lanes=2)
+    srv = serve.Server(ex, hbm_budget=1 << 40, clock=clock, wait=clock.wait)
+    done = srv.serve(reqs + other)
+    by = {r.rid: r for r in done}
+    assert [by[i].steps for i in range(3)] == [300, 700, 900]
+    assert by[0].completed <= by[1].admitted and by[1].completed <= by[2].admitted
+    assert srv.in_use == 0 and not srv.resident and not ex.tracks  # the last request did not keep it
+    srv2 = serve.Server(ex, hbm_budget=1 << 40, clock=clock, wait=clock.wait)
+    kept = [serve.Request(0, clock.t, pieces[0], track_id="u", keep=True)]
+    srv2.serve(kept)
+    assert srv2.in_use == serve.track_bytes(kept[0]) == srv2.resident["u"]
+
+
+@pytest.mark.gpu
+def test_resident_track_extensions_equal_the_whole_track_alone():
+    """A track served in three requests -- the first keeps it on the device,
+    the next two append their steps -- gives, for every request, the smoothing
+    of the track so far, bit for bit; only each request's new steps are
+    uploaded."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    from ultimate_kalman_gb300 import native
+    rng = np.random.default_rng(17)
+    full = serve.serving_track(6000, 6, 3, rng)
+    cuts = [0, 3000, 5000, 6000]
+    pieces = [full.step_range(a, b) for a, b in zip(cuts, cuts[1:])]
+    reqs = [serve.Request(i, 0.0, P, track_id=42, keep=(i < 2)) for i, P in enumerate(pieces)]
+    others = serve.request_stream(6, 1e6, seed=19, dims=(6,), min_len=64, max_len=2000)
+    for j, r in enumerate(others):
+        r.rid = 10 + j
+    ex = serve.GpuExecutor(lanes=2)
+    srv = serve.Server(ex, hbm_budget=1 << 34)
+    done = srv.serve(reqs + others)
+    ex.close()
+    by = {r.rid: r for r in done}
+    for i in range(3):
+        X, _ = native.smooth(full.step_range(0, cuts[i + 1]), covariance=False)
+        np.testing.assert_array_equal(by[i].state, X)
+    assert ex.uploaded_bytes == sum(P.nbytes() for P in pieces) + sum(r.problem.nbytes() for r in others)
+    assert not ex.resident and srv.in_use == 0

@@ -31,6 +31,7 @@
 #include <deque>
 #include <mutex>
 #include <set>
+#include <thread>
 #include <vector>
 
 #include "ukgpu_internal.h"
@@ -312,12 +313,17 @@ extern "C" int64_t kalman_gpu_workspace_held(void)
   return ukg_oddeven_workspace_held() + ukg_associative_workspace_held() + (int64_t)tl_stage.bytes;
 }
 
+namespace {
+void pack_release();
+}
+
 extern "C" void kalman_gpu_release(void)
 {
   ukg_release_oddeven_workspace();
   ukg_release_associative_workspace();
   ukg_release_filter_workspace();
   stage_release(tl_stage);
+  pack_release();
 }
 
 /* -------------------------------------------------------------------------- */
@@ -368,16 +374,59 @@ struct HostPack {
   double *state = nullptr, *cov = nullptr;
   char *Kt = nullptr, *Ct = nullptr;
   int32_t* m = nullptr;
-  void* block = nullptr;
-  bool pinned = false;
-  ~HostPack()
-  {
-    if (block) {
-      if (pinned) cudaFreeHost(block);
-      else free(block);
-    }
-  }
+  void* block = nullptr; /* the calling thread's cached staging buffer (tl_pack) */
 };
+
+/* The packed image of an equations array is staged in one page-locked host
+ * buffer per host thread, kept between calls (grow-only; released by
+ * kalman_gpu_release): page-locking tens of GB on every call would cost more
+ * than the smoothing.                                                        */
+struct PackCache {
+  void* p = nullptr;
+  size_t bytes = 0;
+  bool pinned = false;
+};
+thread_local PackCache tl_pack;
+
+void pack_release()
+{
+  if (tl_pack.p) {
+    if (tl_pack.pinned) cudaFreeHost(tl_pack.p);
+    else free(tl_pack.p);
+  }
+  tl_pack = PackCache();
+}
+
+void* pack_buffer(size_t bytes)
+{
+  if (tl_pack.p && tl_pack.bytes >= bytes) return tl_pack.p;
+  pack_release();
+  if (cudaHostAlloc(&tl_pack.p, bytes, cudaHostAllocDefault) == cudaSuccess) {
+    tl_pack.pinned = true;
+  } else {
+    cudaGetLastError();
+    tl_pack.p = malloc(bytes);
+    tl_pack.pinned = false;
+  }
+  tl_pack.bytes = tl_pack.p ? bytes : 0;
+  return tl_pack.p;
+}
+
+/* f(lo, hi) over [0, N) in contiguous ranges on up to 32 host threads (one
+ * range per 16,384 steps at least); per-step marshalling is independent.    */
+template <class Fn>
+void parallel_steps(int64_t N, Fn f)
+{
+  const int64_t hw = std::max<int64_t>(1, (int64_t)std::thread::hardware_concurrency());
+  const int64_t T = std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(hw, 32), N / 16384));
+  if (T == 1) {
+    f((int64_t)0, N);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (int64_t t = 0; t < T; ++t) pool.emplace_back(f, N * t / T, N * (t + 1) / T);
+  for (auto& th : pool) th.join();
+}
 
 int pack_equations(kalman_step_equations_t** eq, int64_t N, const kalman_step_index_t* lengths, int ntracks,
                    bool want_cov, HostPack& hp, kalman_gpu_problem_t& P)
@@ -385,7 +434,20 @@ int pack_equations(kalman_step_equations_t** eq, int64_t N, const kalman_step_in
   if (!eq) return ukg_set_error(KALMAN_GPU_EINVAL, "equations is NULL");
   for (int64_t s = 0; s < N; ++s)
     if (!eq[s]) return ukg_set_error(KALMAN_GPU_EINVAL, "equations[%lld] is NULL", (long long)s);
-  const int n = eq[0]->dimension;
+  /* Steps may have different state dimensions n_s, and fewer evolution rows
+   * l_s than states (c/kalman.h:56-75; the reference's test catalogue grows
+   * the state, matlab/examples/kalmanTest.m:93-94).  The packed problem has
+   * one dimension, so every step is padded to n = max n_s with dummy
+   * components d_s (slots n_s .. n-1) that no real equation touches: evolution
+   * rows l_s .. n-1 read d_s = 0 * d_{s-1} + e (unit noise, as far as there
+   * are dummy slots; zero rows after that), and every step observes d_s = 0
+   * with unit weight.  The least-squares problem then separates into the
+   * caller's problem and an independent one for the dummies, so the real
+   * components' estimates and covariances are unchanged; they are unpacked at
+   * each step's own size.  Without padding (all n_s = l_s = n) the packed
+   * arrays are exactly the caller's matrices.                              */
+  int n = 0;
+  for (int64_t s = 0; s < N; ++s) n = std::max(n, (int)eq[s]->dimension);
   if (n < 1) return ukg_set_error(KALMAN_GPU_EINVAL, "state dimension %d < 1", n);
   hp.track_start.assign(ntracks + 1, 0);
   for (int t = 0; t < ntracks; ++t) {
@@ -399,38 +461,35 @@ int pack_equations(kalman_step_equations_t** eq, int64_t N, const kalman_step_in
     if (lengths[t] > 0) first[hp.track_start[t]] = 1;
   for (int64_t s = 0; s < N; ++s) {
     const kalman_step_equations_t* e = eq[s];
-    if (e->dimension != n)
-      return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld has dimension %d, step 0 has %d; steps of different "
-                           "dimensions are not supported", (long long)s, e->dimension, n);
+    const int ns = e->dimension;
+    if (ns < 1) return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld has state dimension %d", (long long)s, ns);
     if (!first[s]) {
-      if (rows_of(e->H) != n || cols_of(e->H) != n || rows_of(e->F) != n || cols_of(e->F) != n ||
-          rows_of(e->c) != n || cols_of(e->c) != 1 || !e->H->elements || !e->F->elements || !e->c->elements)
-        return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld: H and F must be %dx%d and c %dx1", (long long)s, n, n, n);
-      if (!valid_cov(e->K, e->K_type, n))
+      const int np = eq[s - 1]->dimension, l = rows_of(e->H);
+      if (l < 1 || l > n || cols_of(e->H) != ns || rows_of(e->F) != l || cols_of(e->F) != np || rows_of(e->c) != l ||
+          cols_of(e->c) != 1 || !e->H->elements || !e->F->elements || !e->c->elements)
+        return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld: H must be l x %d, F l x %d and c l x 1 with 1 <= l <= %d",
+                             (long long)s, ns, np, n);
+      if (!valid_cov(e->K, e->K_type, l))
         return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld: bad evolution covariance (type '%c')", (long long)s,
                              e->K_type ? e->K_type : '?');
     }
+    int m = 0;
     if (e->o) {
-      const int m = rows_of(e->o);
-      if (m < 1 || cols_of(e->o) != 1 || rows_of(e->G) != m || cols_of(e->G) != n || !e->G->elements ||
+      m = rows_of(e->o);
+      if (m < 1 || cols_of(e->o) != 1 || rows_of(e->G) != m || cols_of(e->G) != ns || !e->G->elements ||
           !e->o->elements)
-        return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld: G must be m x %d and o m x 1", (long long)s, n);
+        return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld: G must be m x %d and o m x 1", (long long)s, ns);
       if (!valid_cov(e->C, e->C_type, m))
         return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld: bad observation covariance (type '%c')", (long long)s,
                              e->C_type ? e->C_type : '?');
-      if (m > mmax) mmax = m;
     }
+    mmax = std::max(mmax, m + (n - ns)); /* the observation and the dummies' zero observation */
   }
   const size_t nn = (size_t)n * n, mm = (size_t)mmax;
   const size_t dbl = N * (3 * nn + n + mm * n + mm + mm * mm + n + (want_cov ? nn : 0));
   const size_t bytes = dbl * sizeof(double) + 2 * N + 4 * N + 64;
-  if (cudaHostAlloc(&hp.block, bytes, cudaHostAllocDefault) == cudaSuccess) {
-    hp.pinned = true;
-  } else {
-    cudaGetLastError();
-    hp.block = malloc(bytes);
-    if (!hp.block) return ukg_set_error(KALMAN_GPU_ENOMEM, "host allocation of %zu bytes failed", bytes);
-  }
+  hp.block = pack_buffer(bytes);
+  if (!hp.block) return ukg_set_error(KALMAN_GPU_ENOMEM, "host allocation of %zu bytes failed", bytes);
   double* d = (double*)hp.block;
   hp.H = d; d += N * nn;
   hp.F = d; d += N * nn;
@@ -444,35 +503,59 @@ int pack_equations(kalman_step_equations_t** eq, int64_t N, const kalman_step_in
   hp.m = (int32_t*)d;
   hp.Kt = (char*)(hp.m + N);
   hp.Ct = hp.Kt + N;
-  memset(hp.block, 0, (char*)(hp.Ct + N) - (char*)hp.block);
-  for (int64_t s = 0; s < N; ++s) {
-    const kalman_step_equations_t* e = eq[s];
-    hp.Kt[s] = 'C';
-    hp.Ct[s] = 'C';
-    if (!first[s]) {
-      copy_block(hp.H + s * nn, n, e->H);
-      copy_block(hp.F + s * nn, n, e->F);
-      copy_block(hp.c + s * n, n, e->c);
-      if (e->K_type == 'w') {
-        for (int i = 0; i < n; ++i) hp.K[s * nn + i] = e->K->elements[i];
-      } else {
-        copy_block(hp.K + s * nn, n, e->K);
-      }
-      hp.Kt[s] = e->K_type;
+  /* unit weight on pad rows beyond a covariance block of `rows` (ld) */
+  auto pad_cov = [](double* B, int ld, char type, int rows, int total) {
+    for (int i = rows; i < total; ++i) {
+      if (type == 'w') B[i] = 1.0;
+      else B[(size_t)i * ld + i] = 1.0;
     }
-    if (e->o) {
-      const int m = e->o->row_dim;
-      hp.m[s] = m;
-      copy_block(hp.G + s * mm * n, (int)mm, e->G);
-      for (int i = 0; i < m; ++i) hp.o[s * mm + i] = e->o->elements[i];
-      if (e->C_type == 'w') {
-        for (int i = 0; i < m; ++i) hp.C[s * mm * mm + i] = e->C->elements[i];
-      } else {
-        copy_block(hp.C + s * mm * mm, (int)mm, e->C);
+  };
+  parallel_steps(N, [&](int64_t lo, int64_t hi) {
+    const size_t cnt = (size_t)(hi - lo);
+    memset(hp.H + lo * nn, 0, cnt * nn * sizeof(double));
+    memset(hp.F + lo * nn, 0, cnt * nn * sizeof(double));
+    memset(hp.K + lo * nn, 0, cnt * nn * sizeof(double));
+    memset(hp.c + lo * n, 0, cnt * n * sizeof(double));
+    memset(hp.G + lo * mm * n, 0, cnt * mm * n * sizeof(double));
+    memset(hp.o + lo * mm, 0, cnt * mm * sizeof(double));
+    memset(hp.C + lo * mm * mm, 0, cnt * mm * mm * sizeof(double));
+    for (int64_t s = lo; s < hi; ++s) {
+      const kalman_step_equations_t* e = eq[s];
+      const int ns = e->dimension, dummies = n - ns;
+      hp.Kt[s] = 'C';
+      hp.Ct[s] = 'C';
+      if (!first[s]) {
+        const int l = e->H->row_dim;
+        copy_block(hp.H + s * nn, n, e->H);
+        copy_block(hp.F + s * nn, n, e->F);
+        copy_block(hp.c + s * n, n, e->c);
+        if (e->K_type == 'w') {
+          for (int i = 0; i < l; ++i) hp.K[s * nn + i] = e->K->elements[i];
+        } else {
+          copy_block(hp.K + s * nn, n, e->K);
+        }
+        hp.Kt[s] = e->K_type;
+        pad_cov(hp.K + s * nn, n, e->K_type, l, n);
+        for (int r = l; r < n && r - l < dummies; ++r) hp.H[s * nn + (size_t)(ns + r - l) * n + r] = 1.0;
       }
-      hp.Ct[s] = e->C_type;
+      const int m = e->o ? e->o->row_dim : 0;
+      if (m > 0) {
+        copy_block(hp.G + s * mm * n, (int)mm, e->G);
+        for (int i = 0; i < m; ++i) hp.o[s * mm + i] = e->o->elements[i];
+        if (e->C_type == 'w') {
+          for (int i = 0; i < m; ++i) hp.C[s * mm * mm + i] = e->C->elements[i];
+        } else {
+          copy_block(hp.C + s * mm * mm, (int)mm, e->C);
+        }
+        hp.Ct[s] = e->C_type;
+      }
+      if (dummies > 0) { /* d_s = 0, unit weight */
+        for (int j = 0; j < dummies; ++j) hp.G[s * mm * n + (size_t)(ns + j) * mm + m + j] = 1.0;
+        pad_cov(hp.C + s * mm * mm, (int)mm, hp.Ct[s], m, m + dummies);
+      }
+      hp.m[s] = m + dummies;
     }
-  }
+  });
   memset(&P, 0, sizeof(P));
   P.n = n;
   P.mmax = mmax;
@@ -487,27 +570,33 @@ int pack_equations(kalman_step_equations_t** eq, int64_t N, const kalman_step_in
   return 0;
 }
 
-/* writes the results into the equations (caller-owned matrices, type 'C') */
+/* writes the results into the equations (caller-owned matrices, type 'C'):
+ * each step's leading dimension x dimension part of the packed results,
+ * whose stride is n0 (the padded dimension); one host thread per range      */
 void unpack_results(kalman_step_equations_t** eq, int64_t N, int n0, const double* state, const double* cov,
                     bool failed)
 {
-  for (int64_t s = 0; s < N; ++s) {
-    kalman_step_equations_t* e = eq[s];
-    if (!e) continue;
-    const int n = failed ? e->dimension : n0;
-    if (n < 1) continue;
-    const size_t nn = (size_t)n * n;
-    free_matrix(e->state);
-    free_matrix(e->covariance);
-    e->state = new_matrix(n, 1);
-    for (int i = 0; i < n; ++i) e->state->elements[i] = failed ? NAN : state[s * n + i];
-    e->covariance = nullptr;
-    if (cov || failed) {
-      e->covariance = new_matrix(n, n);
-      for (size_t i = 0; i < nn; ++i) e->covariance->elements[i] = failed ? NAN : cov[s * nn + i];
+  parallel_steps(N, [&](int64_t lo, int64_t hi) {
+    for (int64_t s = lo; s < hi; ++s) {
+      kalman_step_equations_t* e = eq[s];
+      if (!e) continue;
+      const int n = e->dimension;
+      if (n < 1 || (!failed && n > n0)) continue;
+      const size_t nn0 = (size_t)n0 * n0;
+      free_matrix(e->state);
+      free_matrix(e->covariance);
+      e->state = new_matrix(n, 1);
+      for (int i = 0; i < n; ++i) e->state->elements[i] = failed ? NAN : state[s * n0 + i];
+      e->covariance = nullptr;
+      if (cov || failed) {
+        e->covariance = new_matrix(n, n);
+        for (int j = 0; j < n; ++j)
+          for (int i = 0; i < n; ++i)
+            e->covariance->elements[(size_t)j * n + i] = failed ? NAN : cov[s * nn0 + (size_t)j * n0 + i];
+      }
+      e->covariance_type = 'C';
     }
-    e->covariance_type = 'C';
-  }
+  });
 }
 
 int smooth_equations(bool associative, uint32_t options, kalman_step_equations_t** eq, int64_t N,
@@ -520,7 +609,13 @@ int smooth_equations(bool associative, uint32_t options, kalman_step_equations_t
   if (associative) options &= ~(uint32_t)KALMAN_NO_COVARIANCE;
   HostPack hp;
   kalman_gpu_problem_t P;
-  int status = pack_equations(eq, N, lengths, ntracks, want_cov, hp, P);
+  int status = 0;
+  if (associative && eq) /* it takes H as the identity: evolutions must be square (l_s = n_s) */
+    for (int64_t s = 0; s < N && !status; ++s)
+      if (eq[s] && eq[s]->H && eq[s]->H->row_dim != eq[s]->dimension)
+        status = ukg_set_error(KALMAN_GPU_EINVAL, "step %lld: the associative smoother needs as many evolution "
+                               "rows as states (%d, not %d)", (long long)s, eq[s]->dimension, eq[s]->H->row_dim);
+  if (status == 0) status = pack_equations(eq, N, lengths, ntracks, want_cov, hp, P);
   if (status == 0) status = device_ready();
   if (status == 0)
     status = run_host_problem(associative ? ukg_associative_device : ukg_oddeven_device, options, &P, want_cov,

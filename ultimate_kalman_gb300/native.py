@@ -445,6 +445,79 @@ def build_equations(P):
     return arr, keep, structs
 
 
+class EquationsView:
+    """kalman_step_equations_t structs for every step of a PackedProblem,
+    built with numpy in bulk (the matrices point into the problem's packed
+    arrays: blocks are column-major with ld = n, or ld = mmax for G, o, C),
+    for driving the reference entry points on millions of steps.  Keeps the
+    problem alive; results are written into the structs by the library.
+
+    ptrs: the kalman_step_equations_t* array; lengths: the track lengths."""
+
+    def __init__(self, P):
+        fields = {f: np.ascontiguousarray(getattr(P, f)) for f in _FIELDS}
+        self.keep = fields
+        N, n, mm = int(P.nsteps), int(P.n), int(P.mmax)
+        mat = np.dtype({"names": ["rows", "cols", "ld", "elements"], "formats": ["<i4", "<i4", "<i4", "<u8"],
+                        "offsets": [0, 4, 8, 16], "itemsize": ctypes.sizeof(Matrix)})
+        kinds = ["H", "F", "K", "c", "G", "o", "C"]
+        self.mats = np.zeros((len(kinds), N), dtype=mat)
+        first = np.zeros(N, dtype=bool)
+        first[np.asarray(P.track_start[:-1])[np.diff(P.track_start) > 0]] = True
+        m = fields["obs_rows"].astype(np.int32)
+        steps = np.arange(N, dtype=np.uint64)
+        kt, ct = fields["K_type"], fields["C_type"]
+        spec = {"H": (n, n, n, n * n), "F": (n, n, n, n * n), "c": (n, 1, n, n), "G": (m, n, mm, mm * n),
+                "o": (m, 1, mm, mm), "C": (m, np.where(ct == ord("w"), 1, m), mm, mm * mm),
+                "K": (n, np.where(kt == ord("w"), 1, n), n, n * n)}
+        for i, k in enumerate(kinds):
+            rows, cols, ld, per = spec[k]
+            a = self.mats[i]
+            a["rows"], a["cols"], a["ld"] = rows, cols, ld
+            a["elements"] = np.uint64(fields[k].ctypes.data) + steps * np.uint64(per * 8)
+        eqd = np.dtype({"names": [f for f, _ in StepEquations._fields_],
+                        "formats": ["<i4", "<i4", "S1", "S1"] + ["<u8"] * 9 + ["S1"],
+                        "offsets": [getattr(StepEquations, f).offset for f, _ in StepEquations._fields_],
+                        "itemsize": ctypes.sizeof(StepEquations)})
+        self.eq = np.zeros(N, dtype=eqd)
+        self.eq["step"] = np.where(first, 0, 1)
+        self.eq["dimension"] = n
+        self.eq["K_type"] = kt.view("S1")
+        self.eq["C_type"] = ct.view("S1")
+        self.eq["covariance_type"] = b"C"
+        base = np.uint64(self.mats.ctypes.data)
+        sz = np.uint64(ctypes.sizeof(Matrix))
+        for i, k in enumerate(kinds):
+            ptr = base + (np.uint64(i * N) + steps) * sz
+            if k in ("H", "F", "K", "c"):
+                ptr = np.where(first, np.uint64(0), ptr)
+            else:
+                ptr = np.where(m > 0, ptr, np.uint64(0))
+            self.eq[k] = ptr
+        self.ptrs = np.uint64(self.eq.ctypes.data) + steps * np.uint64(ctypes.sizeof(StepEquations))
+        self.lengths = np.ascontiguousarray(np.diff(P.track_start), dtype=np.int32)
+        self.n = n
+
+    def smooth_tracks(self, algorithm="oddeven", covariance=False, fp32_refine=False, sweeps=0):
+        """kalman_gpu_smooth_tracks over every track; returns the status.  The
+        library frees the previous call's result matrices before writing."""
+        L = load()
+        opts = options_for(algorithm, covariance, fp32_refine, sweeps)
+        arr = self.ptrs.ctypes.data_as(ctypes.POINTER(ctypes.POINTER(StepEquations)))
+        lens = self.lengths.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        return L.kalman_gpu_smooth_tracks(opts, arr, lens, len(self.lengths))
+
+    def states(self, steps):
+        """The smoothed states of the given step indices (from the structs)."""
+        out = np.full((len(steps), self.n), np.nan)
+        for j, s in enumerate(steps):
+            p = int(self.eq["state"][s])
+            if p:
+                M = Matrix.from_address(p)
+                out[j] = np.ctypeslib.as_array(M.elements, shape=(self.n,))
+        return out
+
+
 def _read_matrix(mp):
     if not mp:
         return None

@@ -68,6 +68,17 @@ class PackedProblem:
         return PackedProblem(self.n, self.mmax, ts, **kw)
 
 
+    def step_range(self, a, b) -> "PackedProblem":
+        """Steps a .. b-1 of a one-track problem as a one-track problem.  The
+        first of them keeps its evolution arrays: ignored when the piece is
+        smoothed on its own (a track's first step has no evolution), used when
+        it is appended to the steps before it (a resident track extended)."""
+        assert self.ntracks == 1 and 0 <= a < b <= self.nsteps
+        kw = {f: np.ascontiguousarray(getattr(self, f)[a:b]) for f in
+              ("H", "F", "c", "K", "K_type", "G", "o", "C", "C_type", "obs_rows")}
+        return PackedProblem(self.n, self.mmax, np.array([0, b - a], dtype=np.int64), **kw)
+
+
 def empty_problem(n: int, mmax: int, lengths) -> PackedProblem:
     lengths = np.asarray(lengths, dtype=np.int64)
     ts = np.zeros(len(lengths) + 1, dtype=np.int64)

@@ -52,6 +52,9 @@ class Request:
     device: dict = None        # resident device arrays once admitted
     ready: object = None       # CUDA event: the upload has completed
     workspace: int = 0         # library workspace bytes for the request alone
+    track_id: object = None    # a track the server keeps on the device (None: a one-off track)
+    keep: bool = False         # keep the (extended) track resident after answering
+    prior_steps: int = 0       # steps of the resident track this request extends (set at admission)
     admitted: float = None
     started: float = None
     completed: float = None
@@ -60,7 +63,8 @@ class Request:
 
     @property
     def steps(self):
-        return int(self.problem.nsteps)
+        """Steps smoothed for this request: the resident track's and its own."""
+        return int(self.prior_steps + self.problem.nsteps)
 
     def key(self):
         return (self.problem.n, self.problem.mmax, self.covariance, self.fp32_refine)
@@ -73,9 +77,15 @@ def footprint(req: Request) -> int:
     the library's workspace for a batch is the sum over its requests up to
     per-track table entries)."""
     P = req.problem
-    eq = P.nbytes()
-    out = P.nsteps * P.n * 8 * (1 + (P.n if req.covariance else 0))
+    eq = P.nbytes() * req.steps // max(1, P.nsteps)  # the whole (extended) track on the device
+    out = req.steps * P.n * 8 * (1 + (P.n if req.covariance else 0))
     return int(eq + eq + out + req.workspace)
+
+
+def track_bytes(req: Request) -> int:
+    """Device bytes of the request's whole track's equations (what stays
+    resident when the request keeps its track)."""
+    return int(req.problem.nbytes() * req.steps // max(1, req.problem.nsteps))
 
 
 @dataclasses.dataclass
@@ -210,6 +220,8 @@ class GpuExecutor:
         self.t0.record()
         self.intervals = []  # (lane, device ms at start, device ms at end, requests) per finished batch
         self.held = {}       # lane -> device bytes its thread's library workspace holds
+        self.resident = {}   # track id -> (device arrays of the track's equations, steps)
+        self.uploaded_bytes = 0
         self._lock = threading.Lock()
 
     def _struct(self, n, mmax, ts, arrays, state, covs):
@@ -232,18 +244,40 @@ class GpuExecutor:
         s.covariance = 1 if cov else None  # only its presence matters
         return int(self.native.oddeven_workspace_bytes(s, covariance=cov, fp32_refine=f32))
 
+    def resident_steps(self, track_id):
+        return self.resident[track_id][1] if track_id in self.resident else 0
+
     def upload(self, req: Request):
+        """Puts the request's equations on the device.  A request extending a
+        resident track uploads only its own steps; the track is assembled on
+        the device (its first step carries the evolution from the track's last
+        resident step)."""
         torch = self.torch
         with torch.cuda.stream(self.copy_stream):
             if isinstance(req.problem, TrackSpec):
-                req.device = req.problem.materialize(torch, self.device, self.copy_stream)
+                if req.prior_steps:
+                    raise ValueError("a compact request cannot extend a resident track (send packed steps)")
+                mine = req.problem.materialize(torch, self.device, self.copy_stream)
             else:
-                req.device = {f: torch.from_numpy(np.ascontiguousarray(getattr(req.problem, f))).to(
+                mine = {f: torch.from_numpy(np.ascontiguousarray(getattr(req.problem, f))).to(
                     self.device, non_blocking=True) for f in FIELDS}
+                self.uploaded_bytes += req.problem.nbytes()
+            if req.prior_steps:
+                old = self.resident[req.track_id][0]
+                req.device = {f: torch.cat([old[f], mine[f]]) for f in FIELDS}
+            else:
+                req.device = mine
             req.ready = torch.cuda.Event()
             req.ready.record(self.copy_stream)
 
     def release(self, req: Request):
+        """Frees the request's device arrays, or keeps them as its track's
+        resident equations (req.keep)."""
+        if req.track_id is not None:
+            if req.keep:
+                self.resident[req.track_id] = (req.device, req.steps)
+            else:
+                self.resident.pop(req.track_id, None)
         req.device = None
         req.ready = None
 
@@ -314,6 +348,7 @@ class Server:
         self.peak_in_use = 0
         self.batches = []
         self.max_running = 0
+        self.resident = {}  # track id -> device bytes of its resident equations (part of in_use)
         self._t0 = None
         self.clock = clock or self._wall
         self.wait = wait or (lambda dt: time.sleep(max(0.0, min(dt, 0.0005))))
@@ -330,6 +365,7 @@ class Server:
         running = []                                # (future, lane, batch)
         free = list(range(self.lanes))
         done = []
+        busy_tracks = set()  # tracks with a request admitted or running: the next one waits for it
         while pending or queue or any(admitted.values()) or running:
             now = self.clock()
             progressed = False
@@ -337,6 +373,10 @@ class Server:
                 queue.append(pending.popleft())
             while queue:
                 r = queue[0]
+                if r.track_id is not None:
+                    if r.track_id in busy_tracks:
+                        break  # requests of one track are answered in order, each extending the last
+                    r.prior_steps = self.ex.resident_steps(r.track_id) if hasattr(self.ex, "resident_steps") else 0
                 if hasattr(self.ex, "workspace_bytes") and not r.workspace:
                     r.workspace = self.ex.workspace_bytes(r)
                 f = footprint(r)
@@ -346,6 +386,8 @@ class Server:
                     break
                 queue.popleft()
                 self.ex.upload(r)
+                if r.track_id is not None:
+                    busy_tracks.add(r.track_id)
                 r.admitted = self.clock()
                 self.in_use += f
                 self.peak_in_use = max(self.peak_in_use, self.in_use)
@@ -363,6 +405,12 @@ class Server:
                     r.completed = t
                     self.ex.release(r)
                     self.in_use -= footprint(r)
+                    if r.track_id is not None:
+                        busy_tracks.discard(r.track_id)
+                        self.in_use -= self.resident.pop(r.track_id, 0)
+                        if r.keep:
+                            self.resident[r.track_id] = track_bytes(r)
+                            self.in_use += self.resident[r.track_id]
                     done.append(r)
                 progressed = True
             while free:
