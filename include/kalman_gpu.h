@@ -104,6 +104,35 @@ int kalman_gpu_smooth_oddeven_packed    (uint32_t options, const kalman_gpu_prob
 /* Associative-scan (Sarkka-Garcia-Fernandez) smoothing of a packed problem.  */
 int kalman_gpu_smooth_associative_packed(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream);
 
+/* First-step observations apart from the packed rows (no reference
+ * counterpart).  A track's first step often has more observation rows than
+ * its other steps (a prior folded into a square observation: n rows against
+ * m), and the packed layout stores every step with mmax rows -- padding that
+ * is a quarter of the bytes of a 6-state, 3-observation problem.  Here p
+ * describes every step with p->mmax observation rows, except that the first
+ * step of each track takes its observation from f0 (arrays in the same
+ * location as p's; the first steps' own G, o, C, C_type, obs_rows slots are
+ * ignored):
+ *   G0         [ntracks][m0max*n]      ld = m0max
+ *   o0         [ntracks][m0max]
+ *   C0         [ntracks][m0max*m0max]  ld = m0max, type C0_type[t]
+ *   C0_type    [ntracks]
+ *   obs_rows0  [ntracks]               rows of track t's first observation
+ * The odd-even smoother then runs as kalman_gpu_smooth_oddeven_packed would
+ * on the padded problem (the same results, bit for bit): with host arrays the
+ * library copies the compact arrays and pads them on the device, so the host
+ * link carries no padding.                                                   */
+typedef struct kalman_gpu_first_obs_st {
+  int32_t m0max;
+  const double*  G0;
+  const double*  o0;
+  const double*  C0;
+  const char*    C0_type;
+  const int32_t* obs_rows0;
+} kalman_gpu_first_obs_t;
+int kalman_gpu_smooth_oddeven_first_obs(uint32_t options, const kalman_gpu_problem_t* p,
+                                        const kalman_gpu_first_obs_t* f0, void* cuda_stream);
+
 /* Batched form of kalman_smooth_oddeven / kalman_smooth_associative: the
  * equations of ntracks independent tracks are stored one track after the
  * other; track t has track_lengths[t] steps.  Results are written into the

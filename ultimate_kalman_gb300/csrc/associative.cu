@@ -801,8 +801,7 @@ int ensure(size_t bytes, void** out, cudaStream_t st)
   }
   if (!tl_ws.dev) {
     size_t want = ukg_with_slack(bytes);
-    if (cudaMallocAsync(&tl_ws.dev, want, st) != cudaSuccess) {
-      cudaGetLastError();
+    if (ukg_malloc_async(&tl_ws.dev, want, st) != 0) {
       tl_ws = Workspace();
       return ukg_set_error(KALMAN_GPU_ENOMEM, "cudaMalloc of %zu bytes of workspace failed", want);
     }

@@ -82,6 +82,67 @@ __global__ void expand_steps(char* __restrict__ kt, char* __restrict__ ct, int32
   }
 }
 
+/* Observation blocks of ld rows_s (compact) re-laid with ld rows_d >= rows_s:
+ * dst[s][j * rows_d + r] = src[s][j * cols_s... ] inside the source block,
+ * zero outside.  One thread per destination entry, grid-stride.            */
+__global__ void pad_blocks(double* __restrict__ dst, const double* __restrict__ src, int64_t nsteps, int rows_d,
+                           int cols_d, int rows_s, int cols_s)
+{
+  const int per = rows_d * cols_d;
+  const int64_t total = nsteps * per;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = e / per;
+    const int w = (int)(e - s * per), j = w / rows_d, r = w - j * rows_d;
+    dst[e] = (r < rows_s && j < cols_s) ? src[s * rows_s * cols_s + (int64_t)j * rows_s + r] : 0.0;
+  }
+}
+
+/* covariance types and row counts; a row count outside [0, rows_s] becomes
+ * -1, which the smoother's weighing reports as malformed input             */
+__global__ void pad_steps(char* __restrict__ ct, int32_t* __restrict__ rows, const char* __restrict__ ct_s,
+                          const int32_t* __restrict__ rows_s, int64_t nsteps, int mc)
+{
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nsteps; s += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t m = rows_s[s];
+    ct[s] = ct_s[s];
+    rows[s] = (m >= 0 && m <= mc) ? m : -1;
+  }
+}
+
+/* each track's first-step observation (G0, o0, C0 with ld m0max, type, rows)
+ * written over the padded blocks of its first step first[t] (-1: an empty
+ * track)                                                                    */
+__global__ void place_first_obs(double* __restrict__ G, double* __restrict__ o, double* __restrict__ C,
+                                char* __restrict__ ct, int32_t* __restrict__ rows, const int64_t* __restrict__ first,
+                                int ntracks, int n, int mp, const double* __restrict__ G0, const double* __restrict__ o0,
+                                const double* __restrict__ C0, const char* __restrict__ C0t,
+                                const int32_t* __restrict__ rows0, int m0max)
+{
+  const int per = mp * n + mp + mp * mp;
+  const int64_t total = (int64_t)ntracks * per;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int t = (int)(e / per);
+    const int w = (int)(e - (int64_t)t * per);
+    const int64_t s = first[t];
+    if (s < 0) continue;
+    if (w < mp * n) {
+      const int j = w / mp, r = w - j * mp;
+      G[s * mp * n + w] = r < m0max ? G0[(int64_t)t * m0max * n + (int64_t)j * m0max + r] : 0.0;
+    } else if (w < mp * n + mp) {
+      const int r = w - mp * n;
+      o[s * mp + r] = r < m0max ? o0[(int64_t)t * m0max + r] : 0.0;
+    } else {
+      const int w2 = w - mp * n - mp, j = w2 / mp, r = w2 - j * mp;
+      C[s * mp * mp + w2] = (r < m0max && j < m0max) ? C0[(int64_t)t * m0max * m0max + (int64_t)j * m0max + r] : 0.0;
+    }
+    if (w == 0) {
+      const int32_t m = rows0[t];
+      ct[s] = C0t[t];
+      rows[s] = (m >= 0 && m <= m0max) ? m : -1;
+    }
+  }
+}
+
 unsigned blocks_for(int64_t total)
 {
   int dev = 0, sms = 0;
@@ -146,5 +207,33 @@ extern "C" int kalman_gpu_expand_invariant(const kalman_gpu_problem_t* p, int64_
                                   md->m0, md->m, obs_rows)));
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return ukg_set_error(KALMAN_GPU_ECUDA, "expand_invariant: %s", cudaGetErrorString(e));
+  return KALMAN_GPU_OK;
+}
+
+/* Lays out the observations of a problem whose steps carry mc = p->mmax rows
+ * and whose tracks' first-step observations come from f0, as the ordinary
+ * packed layout with mp >= max(mc, f0->m0max) rows: G, o, C, C_type and
+ * obs_rows of every step into the given device arrays (first[t]: the first
+ * step of track t, -1 for an empty track, a device array).  Queued on st.  */
+extern "C" int ukg_pad_first_obs(const kalman_gpu_problem_t* p, const kalman_gpu_first_obs_t* f0, int mp, double* G,
+                                 double* o, double* C, char* ct, int32_t* rows, const int64_t* first, void* cuda_stream)
+{
+  cudaStream_t st = (cudaStream_t)cuda_stream;
+  const int n = p->n, mc = p->mmax;
+  const int64_t N = p->nsteps;
+  UKG_LAUNCH(UKG_K_BUILD, st, (pad_blocks<<<blocks_for(N * mp * n), kBuildThreads, 0, st>>>(
+                                  G, p->G, N, mp, n, mc, n)));
+  UKG_LAUNCH(UKG_K_BUILD, st, (pad_blocks<<<blocks_for(N * mp), kBuildThreads, 0, st>>>(
+                                  o, p->o, N, mp, 1, mc, 1)));
+  UKG_LAUNCH(UKG_K_BUILD, st, (pad_blocks<<<blocks_for(N * mp * mp), kBuildThreads, 0, st>>>(
+                                  C, p->C, N, mp, mp, mc, mc)));
+  UKG_LAUNCH(UKG_K_BUILD, st, (pad_steps<<<blocks_for(N), kBuildThreads, 0, st>>>(
+                                  ct, rows, p->C_type, p->obs_rows, N, mc)));
+  const int per = mp * n + mp + mp * mp;
+  UKG_LAUNCH(UKG_K_BUILD, st, (place_first_obs<<<blocks_for((int64_t)p->ntracks * per), kBuildThreads, 0, st>>>(
+                                  G, o, C, ct, rows, first, p->ntracks, n, mp, f0->G0, f0->o0, f0->C0, f0->C0_type,
+                                  f0->obs_rows0, f0->m0max)));
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return ukg_set_error(KALMAN_GPU_ECUDA, "first-step observations: %s", cudaGetErrorString(e));
   return KALMAN_GPU_OK;
 }

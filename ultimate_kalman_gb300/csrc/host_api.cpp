@@ -143,8 +143,93 @@ typedef int (*device_smoother)(uint32_t, const kalman_gpu_problem_t*, void*);
  * stream while chunk k-1 is smoothed on the caller's stream, and its states
  * (and covariances) are copied back on a second copy stream while chunk k+1
  * is smoothed -- so the host link, which bounds this path, stays busy.      */
-int run_host_problem(device_smoother fn, uint32_t options, const kalman_gpu_problem_t* p, bool want_cov,
+/* The padded observation arrays of kalman_gpu_smooth_oddeven_first_obs on
+ * the device (one buffer per host thread, grown by stream-ordered
+ * allocation), and the tracks' first-step indices staged in page-locked host
+ * memory (every call synchronizes its stream before returning, so the next
+ * call may refill them).                                                     */
+struct PadCache {
+  int device = -1;
+  void* dev = nullptr;
+  size_t bytes = 0;
+  int64_t* idx = nullptr;
+  size_t idx_cap = 0;
+};
+thread_local PadCache tl_pad;
+
+void pad_release()
+{
+  if (tl_pad.dev) cudaFree(tl_pad.dev);
+  if (tl_pad.idx) cudaFreeHost(tl_pad.idx);
+  tl_pad = PadCache();
+}
+
+/* kalman_gpu_smooth_oddeven_first_obs on device arrays: pads the compact
+ * observations (p->mmax rows, first steps from f0) to the packed layout with
+ * max(p->mmax, f0->m0max) rows, then runs the odd-even smoother on it.      */
+int first_obs_device(uint32_t options, const kalman_gpu_problem_t* p, const kalman_gpu_first_obs_t* f0,
                      cudaStream_t st)
+{
+  const int64_t N = p->nsteps, n = p->n;
+  const int T = p->ntracks;
+  const int mp = std::max(p->mmax, f0->m0max);
+  size_t off[6], bytes = 0;
+  const size_t sz[6] = {(size_t)N * mp * n * 8, (size_t)N * mp * 8, (size_t)N * mp * mp * 8, (size_t)N, (size_t)N * 4,
+                        (size_t)std::max(T, 1) * 8};
+  for (int i = 0; i < 6; ++i) {
+    off[i] = bytes;
+    bytes = align_up(bytes + sz[i], 256);
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  PadCache& c = tl_pad;
+  if (c.dev && (c.bytes < bytes || c.device != dev)) {
+    if (c.device == dev) cudaFreeAsync(c.dev, st);
+    else cudaFree(c.dev);
+    c.dev = nullptr;
+    c.bytes = 0;
+  }
+  if (!c.dev) {
+    const size_t want = ukg_with_slack(bytes);
+    if (ukg_malloc_async(&c.dev, want, st) != 0) {
+      c.dev = nullptr;
+      return ukg_set_error(KALMAN_GPU_ENOMEM, "padded observations: %zu bytes of device memory", want);
+    }
+    c.bytes = want;
+    c.device = dev;
+  }
+  if (c.idx_cap < (size_t)std::max(T, 1)) {
+    if (c.idx) cudaFreeHost(c.idx);
+    c.idx = nullptr;
+    c.idx_cap = 0;
+    if (cudaHostAlloc((void**)&c.idx, (size_t)std::max(T, 1) * 8, cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      c.idx = nullptr;
+      return ukg_set_error(KALMAN_GPU_ENOMEM, "page-locked first-step table");
+    }
+    c.idx_cap = (size_t)std::max(T, 1);
+  }
+  for (int t = 0; t < T; ++t) c.idx[t] = p->track_start[t + 1] > p->track_start[t] ? p->track_start[t] : -1;
+  char* B = (char*)c.dev;
+  int64_t* first = (int64_t*)(B + off[5]);
+  cudaMemcpyAsync(first, c.idx, (size_t)std::max(T, 1) * 8, cudaMemcpyHostToDevice, st);
+  double *G = (double*)(B + off[0]), *o = (double*)(B + off[1]), *C = (double*)(B + off[2]);
+  char* ct = (char*)(B + off[3]);
+  int32_t* rows = (int32_t*)(B + off[4]);
+  if (int e = ukg_pad_first_obs(p, f0, mp, G, o, C, ct, rows, first, st)) return e;
+  kalman_gpu_problem_t d = *p;
+  d.location = KALMAN_GPU_DEVICE;
+  d.mmax = mp;
+  d.G = G;
+  d.o = o;
+  d.C = C;
+  d.C_type = ct;
+  d.obs_rows = rows;
+  return ukg_oddeven_device(options, &d, st);
+}
+
+int run_host_problem(device_smoother fn, uint32_t options, const kalman_gpu_problem_t* p, bool want_cov,
+                     cudaStream_t st, const kalman_gpu_first_obs_t* f0 = nullptr)
 {
   const int64_t N = p->nsteps, n = p->n, mm = p->mmax;
   /* chunks of whole tracks */
@@ -154,9 +239,11 @@ int run_host_problem(device_smoother fn, uint32_t options, const kalman_gpu_prob
     if (p->track_start[t] - p->track_start[cut.back()] >= target) cut.push_back(t);
   cut.push_back(p->ntracks);
   const int nchunks = (int)cut.size() - 1;
-  int64_t cmax = 0;
-  for (int k = 0; k < nchunks; ++k)
+  int64_t cmax = 0, tmax = 0;
+  for (int k = 0; k < nchunks; ++k) {
     cmax = std::max<int64_t>(cmax, p->track_start[cut[k + 1]] - p->track_start[cut[k]]);
+    tmax = std::max<int64_t>(tmax, cut[k + 1] - cut[k]);
+  }
 
   /* bytes per step of each array: H F c K K_type G o C C_type obs_rows | state cov */
   const size_t per[12] = {(size_t)(n * n * 8), (size_t)(n * n * 8), (size_t)(n * 8), (size_t)(n * n * 8), 1,
@@ -168,6 +255,17 @@ int run_host_problem(device_smoother fn, uint32_t options, const kalman_gpu_prob
     off[i] = half;
     half = align_up(half + per[i] * (size_t)cmax, 256);
   }
+  /* with separate first-step observations, bytes per track of G0 o0 C0 C0_type obs_rows0 */
+  const int64_t m0 = f0 ? f0->m0max : 0;
+  const size_t per0[5] = {(size_t)(m0 * n * 8), (size_t)(m0 * 8), (size_t)(m0 * m0 * 8), 1, 4};
+  const void* src0[5] = {f0 ? f0->G0 : nullptr, f0 ? f0->o0 : nullptr, f0 ? f0->C0 : nullptr,
+                         f0 ? f0->C0_type : nullptr, f0 ? f0->obs_rows0 : nullptr};
+  size_t off0[5] = {0, 0, 0, 0, 0};
+  if (f0)
+    for (int i = 0; i < 5; ++i) {
+      off0[i] = half;
+      half = align_up(half + per0[i] * (size_t)tmax, 256);
+    }
   int dev = 0;
   cudaGetDevice(&dev);
   Stage& S = tl_stage;
@@ -199,6 +297,10 @@ int run_host_problem(device_smoother fn, uint32_t options, const kalman_gpu_prob
       if (per[i] && src[i])
         cudaMemcpyAsync(D + off[i], (const char*)src[i] + (size_t)g0 * per[i], (size_t)(g1 - g0) * per[i],
                         cudaMemcpyHostToDevice, S.h2d);
+    if (f0)
+      for (int i = 0; i < 5; ++i)
+        cudaMemcpyAsync(D + off0[i], (const char*)src0[i] + (size_t)cut[k] * per0[i],
+                        (size_t)(cut[k + 1] - cut[k]) * per0[i], cudaMemcpyHostToDevice, S.h2d);
     cudaEventRecord(S.h2d_done[k & 1], S.h2d);
   };
   bool used[2] = {false, false};
@@ -231,7 +333,18 @@ int run_host_problem(device_smoother fn, uint32_t options, const kalman_gpu_prob
     d.covariance = want_cov ? (double*)(D + off[11]) : nullptr;
     cudaStreamWaitEvent(st, S.h2d_done[b], 0);
     if (used[b]) cudaStreamWaitEvent(st, S.d2h_done[b], 0); /* chunk k-2's outputs are read back */
-    const int s = fn(options, &d, st);                    /* returns after the smoothing completed */
+    int s;
+    if (f0) {
+      kalman_gpu_first_obs_t fc = *f0;
+      fc.G0 = (const double*)(D + off0[0]);
+      fc.o0 = (const double*)(D + off0[1]);
+      fc.C0 = (const double*)(D + off0[2]);
+      fc.C0_type = (const char*)(D + off0[3]);
+      fc.obs_rows0 = (const int32_t*)(D + off0[4]);
+      s = first_obs_device(options, &d, &fc, st); /* returns after the smoothing completed */
+    } else {
+      s = fn(options, &d, st);
+    }
     if (s == KALMAN_GPU_ECUDA) {
       cudaStreamSynchronize(S.h2d);
       cudaStreamSynchronize(S.d2h);
@@ -277,6 +390,21 @@ extern "C" int kalman_gpu_smooth_oddeven_packed(uint32_t options, const kalman_g
   return smooth_packed(ukg_oddeven_device, options, p, cuda_stream);
 }
 
+extern "C" int kalman_gpu_smooth_oddeven_first_obs(uint32_t options, const kalman_gpu_problem_t* p,
+                                                   const kalman_gpu_first_obs_t* f0, void* cuda_stream)
+{
+  ukg_clear_error();
+  if (!f0 || f0->m0max < 1 || !f0->G0 || !f0->o0 || !f0->C0 || !f0->C0_type || !f0->obs_rows0)
+    return ukg_set_error(KALMAN_GPU_EINVAL, "first-step observations: m0max >= 1 and every array are needed");
+  if (int e = ukg_validate_problem(p, 0)) return e;
+  if (p->nsteps == 0) return 0;
+  if (int e = device_ready()) return e;
+  const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
+  cudaStream_t st = (cudaStream_t)cuda_stream;
+  if (p->location == KALMAN_GPU_HOST) return run_host_problem(ukg_oddeven_device, options, p, want_cov, st, f0);
+  return first_obs_device(options, p, f0, st);
+}
+
 extern "C" int kalman_gpu_smooth_associative_packed(uint32_t options, const kalman_gpu_problem_t* p,
                                                     void* cuda_stream)
 {
@@ -308,9 +436,32 @@ extern "C" void ukg_allow_dynamic_smem(const void* kernel)
   cudaGetLastError();
 }
 
+extern "C" void ukg_trim_pool(void)
+{
+  int dev = 0;
+  cudaMemPool_t pool;
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+    cudaMemPoolTrimTo(pool, 0);
+  cudaGetLastError();
+}
+
+extern "C" int ukg_malloc_async(void** ptr, size_t bytes, void* cuda_stream)
+{
+  cudaStream_t st = (cudaStream_t)cuda_stream;
+  cudaError_t e = cudaMallocAsync(ptr, bytes, st);
+  if (e == cudaSuccess) return 0;
+  cudaGetLastError();
+  cudaStreamSynchronize(st);
+  ukg_trim_pool();
+  e = cudaMallocAsync(ptr, bytes, st);
+  if (e != cudaSuccess) cudaGetLastError();
+  return (int)e;
+}
+
 extern "C" int64_t kalman_gpu_workspace_held(void)
 {
-  return ukg_oddeven_workspace_held() + ukg_associative_workspace_held() + (int64_t)tl_stage.bytes;
+  return ukg_oddeven_workspace_held() + ukg_associative_workspace_held() + (int64_t)tl_stage.bytes +
+         (int64_t)tl_pad.bytes;
 }
 
 namespace {
@@ -324,6 +475,8 @@ extern "C" void kalman_gpu_release(void)
   ukg_release_filter_workspace();
   stage_release(tl_stage);
   pack_release();
+  pad_release();
+  ukg_trim_pool();
 }
 
 /* -------------------------------------------------------------------------- */

@@ -2872,9 +2872,9 @@ int ensure_workspace(size_t bytes, void** out, cudaStream_t st)
   }
   if (!w.dev) {
     size_t want = ukg_with_slack(bytes);
-    cudaError_t e = cudaMallocAsync(&w.dev, want, st);
+    const cudaError_t e = (cudaError_t)ukg_malloc_async(&w.dev, want, st);
     if (e != cudaSuccess) {
-      cudaGetLastError();
+      w.dev = nullptr;
       return ukg_set_error(KALMAN_GPU_ENOMEM, "cudaMalloc of %zu bytes of workspace failed: %s", want,
                            cudaGetErrorString(e));
     }

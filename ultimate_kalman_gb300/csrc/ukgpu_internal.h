@@ -35,6 +35,17 @@ int ukg_validate_problem(const kalman_gpu_problem_t* p, int need_cov);
  * raced between host threads smoothing different shapes (one thread lowered
  * the limit just before another launched a larger request).              */
 void ukg_allow_dynamic_smem(const void* kernel);
+/* cudaMallocAsync from the device's default pool; if that fails, waits for
+ * the stream, returns the pool's unused memory to the device (memory freed by
+ * earlier workspaces stays reserved in the pool until trimmed) and tries once
+ * more.  Returns the CUDA error code (0 on success).                         */
+int ukg_malloc_async(void** ptr, size_t bytes, void* cuda_stream);
+/* returns the default pool's unused memory of the current device            */
+void ukg_trim_pool(void);
+/* builder.cu: the padded observation layout of a problem with separate
+ * first-step observations (kalman_gpu_smooth_oddeven_first_obs)            */
+int ukg_pad_first_obs(const kalman_gpu_problem_t* p, const kalman_gpu_first_obs_t* f0, int mp, double* G, double* o,
+                      double* C, char* ct, int32_t* rows, const int64_t* first, void* cuda_stream);
 /* Workspace bytes to allocate for a problem needing `bytes`: 1/8 more, so a
  * slightly larger next problem reuses it, but at most 1 GiB more (a 150 GB
  * workspace must not hold 19 GB it will never use).                          */

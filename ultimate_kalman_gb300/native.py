@@ -69,6 +69,12 @@ class ProblemStruct(ctypes.Structure):
     ]
 
 
+class FirstObs(ctypes.Structure):
+    """kalman_gpu_first_obs_t (include/kalman_gpu.h)."""
+    _fields_ = [("m0max", ctypes.c_int32), ("G0", ctypes.c_void_p), ("o0", ctypes.c_void_p), ("C0", ctypes.c_void_p),
+                ("C0_type", ctypes.c_void_p), ("obs_rows0", ctypes.c_void_p)]
+
+
 class Tuning(ctypes.Structure):
     """kalman_gpu_tuning_t (include/kalman_gpu.h)."""
     _fields_ = [("cta_min_n", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("pair_block", ctypes.c_int32),
@@ -111,6 +117,7 @@ EXPORTED = [
     "kalman_gpu_plan_create", "kalman_gpu_plan_execute", "kalman_gpu_plan_status", "kalman_gpu_plan_destroy",
     "kalman_gpu_expand_invariant", "kalman_gpu_filter_packed", "kalman_gpu_oddeven_workspace_bytes",
     "kalman_gpu_workspace_held", "kalman_gpu_set_tuning", "kalman_gpu_get_tuning",
+    "kalman_gpu_smooth_oddeven_first_obs",
 ]
 
 _lib = None
@@ -158,6 +165,8 @@ def load(path=LIB_PATH):
     L.kalman_gpu_oddeven_workspace_bytes.argtypes = [ctypes.c_uint32, P]
     L.kalman_gpu_oddeven_workspace_bytes.restype = ctypes.c_int64
     L.kalman_gpu_workspace_held.restype = ctypes.c_int64
+    L.kalman_gpu_smooth_oddeven_first_obs.argtypes = [ctypes.c_uint32, P, ctypes.POINTER(FirstObs), ctypes.c_void_p]
+    L.kalman_gpu_smooth_oddeven_first_obs.restype = ctypes.c_int
     L.kalman_gpu_set_tuning.argtypes = [ctypes.POINTER(Tuning)]
     L.kalman_gpu_set_tuning.restype = ctypes.c_int
     L.kalman_gpu_get_tuning.argtypes = [ctypes.POINTER(Tuning)]
@@ -236,6 +245,56 @@ def get_tuning():
     t = Tuning()
     load().kalman_gpu_get_tuning(ctypes.byref(t))
     return t.as_dict()
+
+
+FIRST_OBS_FIELDS = ("G0", "o0", "C0", "C0_type", "obs_rows0")
+
+
+def first_obs_struct(F0, arrays):
+    """kalman_gpu_first_obs_t over the arrays (numpy or torch, host or
+    device) of a problem.split_first_obs dictionary."""
+    f = FirstObs()
+    f.m0max = int(F0["m0max"])
+    for k in FIRST_OBS_FIELDS:
+        a = arrays[k]
+        setattr(f, k, a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data)
+    return f
+
+
+def smooth_first_obs(Pc, F0, covariance=True, fp32_refine=False, location="device", sweeps=0):
+    """kalman_gpu_smooth_oddeven_first_obs on a problem in first-step-
+    observation form (problem.split_first_obs); returns (states, covs or
+    None) like smooth()."""
+    import torch
+    L = load()
+    N, n = Pc.nsteps, Pc.n
+    opts = options_for("oddeven", covariance, fp32_refine, sweeps)
+    if location == "device":
+        D = DeviceProblem(Pc, covariance)
+        f0a = {k: torch.from_numpy(np.ascontiguousarray(F0[k])).cuda() for k in FIRST_OBS_FIELDS}
+        f = first_obs_struct(F0, f0a)
+        st = torch.cuda.current_stream()
+        _check(L.kalman_gpu_smooth_oddeven_first_obs(opts, ctypes.byref(D.struct), ctypes.byref(f),
+                                                     ctypes.c_void_p(st.cuda_stream)))
+        torch.cuda.synchronize()
+        return D.results() if covariance else (D.state.cpu().numpy(), None)
+    state = np.full((N, n), np.nan)
+    cov = np.full((N, n, n), np.nan) if covariance else None
+    arrs = {f_: np.ascontiguousarray(getattr(Pc, f_)) for f_ in _FIELDS}
+    s = ProblemStruct()
+    s.n, s.mmax, s.ntracks, s.location, s.nsteps = Pc.n, Pc.mmax, Pc.ntracks, KALMAN_GPU_HOST, N
+    ts = np.ascontiguousarray(Pc.track_start, dtype=np.int64)
+    s.track_start = ts.ctypes.data
+    for f_ in _FIELDS:
+        setattr(s, f_, arrs[f_].ctypes.data)
+    s.state = state.ctypes.data
+    s.covariance = cov.ctypes.data if cov is not None else None
+    f0a = {k: np.ascontiguousarray(F0[k]) for k in FIRST_OBS_FIELDS}
+    f = first_obs_struct(F0, f0a)
+    _check(L.kalman_gpu_smooth_oddeven_first_obs(opts, ctypes.byref(s), ctypes.byref(f), None))
+    if cov is not None:
+        cov = np.ascontiguousarray(cov.transpose(0, 2, 1))
+    return state, cov
 
 
 def release():

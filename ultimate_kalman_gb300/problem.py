@@ -79,6 +79,41 @@ class PackedProblem:
         return PackedProblem(self.n, self.mmax, np.array([0, b - a], dtype=np.int64), **kw)
 
 
+def split_first_obs(P: PackedProblem):
+    """The first-step-observation form of a packed problem
+    (kalman_gpu_smooth_oddeven_first_obs): (Pc, F0) where Pc stores every
+    step's observation with as many rows as the other steps need (the tracks'
+    first steps' slots zero) and F0 holds each track's first observation with
+    ld m0max = the largest first-step row count.  Same equations, fewer bytes
+    when the first steps carry more rows (a folded square prior)."""
+    ts = np.asarray(P.track_start)
+    T, n = P.ntracks, P.n
+    firsts = ts[:-1][np.diff(ts) > 0]
+    rest = np.ones(P.nsteps, dtype=bool)
+    rest[firsts] = False
+    mc = max(1, int(P.obs_rows[rest].max()) if rest.any() else 1)
+    m0 = max(1, int(P.obs_rows[firsts].max()) if len(firsts) else 1)
+    mx = P.mmax
+    Pc = PackedProblem(n, mc, ts.copy(), P.H, P.F, P.c, P.K, P.K_type,
+                       np.ascontiguousarray(P.G.reshape(-1, n, mx)[:, :, :mc]),
+                       np.ascontiguousarray(P.o[:, :mc]),
+                       np.ascontiguousarray(P.C.reshape(-1, mx, mx)[:, :mc, :mc]),
+                       P.C_type.copy(), P.obs_rows.copy())
+    # first steps: their packed slots are ignored; keep them zero
+    Pc.G[firsts], Pc.o[firsts], Pc.C[firsts], Pc.obs_rows[firsts] = 0.0, 0.0, 0.0, 0
+    F0 = {"m0max": m0, "G0": np.zeros((T, n, m0)), "o0": np.zeros((T, m0)), "C0": np.zeros((T, m0, m0)),
+          "C0_type": np.full(T, ord("C"), dtype=np.uint8), "obs_rows0": np.zeros(T, dtype=np.int32)}
+    for t in range(T):
+        if ts[t + 1] > ts[t]:
+            s0 = ts[t]
+            F0["G0"][t] = P.G[s0][:, :m0]
+            F0["o0"][t] = P.o[s0][:m0]
+            F0["C0"][t] = P.C[s0][:m0, :m0]
+            F0["C0_type"][t] = P.C_type[s0]
+            F0["obs_rows0"][t] = P.obs_rows[s0]
+    return Pc, F0
+
+
 def empty_problem(n: int, mmax: int, lengths) -> PackedProblem:
     lengths = np.asarray(lengths, dtype=np.int64)
     ts = np.zeros(len(lengths) + 1, dtype=np.int64)
