@@ -316,6 +316,7 @@ def run_gpu(args):
     if plan.status() != 0:
         raise RuntimeError("the plan's smoothing reported %s" % (native.last_error(),))
     plan.close()
+    del plan
     launches = int(round(launches_per * args.steps))
     X32 = D.state.clone()
     if world > 1:

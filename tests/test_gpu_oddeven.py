@@ -217,3 +217,20 @@ def test_bulk_structs_through_the_batched_reference_entry_equal_the_packed_path(
         for _ in range(2):
             assert V.smooth_tracks("oddeven", fp32_refine=f32) == 0, native.last_error()
             np.testing.assert_array_equal(V.states(np.arange(P.nsteps)), Xp)
+
+
+@pytest.mark.parametrize("n,m", [(4, 2), (6, 3), (6, 6)])
+def test_register_tiled_covariance_solve_at_every_level(n, m, parity_log):
+    """n = 4 and 6 run the covariance back-substitution register-tiled
+    (solve_cov_reg_kernel): FP64 and double-float against the oracle at
+    every recursion parity pattern, with missing observations."""
+    lens = [1, 2, 3, 5, 8, 17, 33, 64, 129, 700]
+    P = (pb.constant_velocity(lens, seed=51, missing=0.1) if (n, m) == (6, 3)
+         else pb.random_dynamics(lens, n, m, seed=52 + n + m, missing=0.1))
+    st, Xo, So = oracle.smooth(P, "oddeven")
+    assert st == 0
+    for f32 in (False, True):
+        X, S = native.smooth(P, "oddeven", covariance=True, fp32_refine=f32)
+        ex, es = oracle.rel_err_states(X, Xo), oracle.rel_err_covs(S, So)
+        parity_log(f"register-tiled covariance n={n} m={m} {'double-float' if f32 else 'FP64'}", states=ex, covs=es)
+        assert ex < (1e-9 if f32 else 1e-11) and es < (1e-9 if f32 else 1e-11), (f32, ex, es)

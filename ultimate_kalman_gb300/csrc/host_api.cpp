@@ -145,14 +145,17 @@ typedef int (*device_smoother)(uint32_t, const kalman_gpu_problem_t*, void*);
  * is smoothed -- so the host link, which bounds this path, stays busy.      */
 /* The padded observation arrays of kalman_gpu_smooth_oddeven_first_obs on
  * the device (one buffer per host thread, grown by stream-ordered
- * allocation), and the tracks' first-step indices staged in page-locked host
- * memory (every call synchronizes its stream before returning, so the next
- * call may refill them).                                                     */
+ * allocation), and the tracks' first-step indices in page-locked, device-
+ * mapped host memory, read by the padding kernel itself: a copy on the
+ * compute stream would queue on the copy engine behind the next chunk's
+ * arrays and stall the smoothing.  Every call synchronizes its stream before
+ * returning, so the next call may refill the indices.                        */
 struct PadCache {
   int device = -1;
   void* dev = nullptr;
   size_t bytes = 0;
   int64_t* idx = nullptr;
+  int64_t* idx_dev = nullptr;
   size_t idx_cap = 0;
 };
 thread_local PadCache tl_pad;
@@ -173,10 +176,9 @@ int first_obs_device(uint32_t options, const kalman_gpu_problem_t* p, const kalm
   const int64_t N = p->nsteps, n = p->n;
   const int T = p->ntracks;
   const int mp = std::max(p->mmax, f0->m0max);
-  size_t off[6], bytes = 0;
-  const size_t sz[6] = {(size_t)N * mp * n * 8, (size_t)N * mp * 8, (size_t)N * mp * mp * 8, (size_t)N, (size_t)N * 4,
-                        (size_t)std::max(T, 1) * 8};
-  for (int i = 0; i < 6; ++i) {
+  size_t off[5], bytes = 0;
+  const size_t sz[5] = {(size_t)N * mp * n * 8, (size_t)N * mp * 8, (size_t)N * mp * mp * 8, (size_t)N, (size_t)N * 4};
+  for (int i = 0; i < 5; ++i) {
     off[i] = bytes;
     bytes = align_up(bytes + sz[i], 256);
   }
@@ -200,19 +202,21 @@ int first_obs_device(uint32_t options, const kalman_gpu_problem_t* p, const kalm
   }
   if (c.idx_cap < (size_t)std::max(T, 1)) {
     if (c.idx) cudaFreeHost(c.idx);
-    c.idx = nullptr;
+    c.idx = c.idx_dev = nullptr;
     c.idx_cap = 0;
-    if (cudaHostAlloc((void**)&c.idx, (size_t)std::max(T, 1) * 8, cudaHostAllocDefault) != cudaSuccess) {
+    cudaError_t e = cudaHostAlloc((void**)&c.idx, (size_t)std::max(T, 1) * 8, cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&c.idx_dev, c.idx, 0);
+    if (e != cudaSuccess) {
       cudaGetLastError();
-      c.idx = nullptr;
+      if (c.idx) cudaFreeHost(c.idx);
+      c.idx = c.idx_dev = nullptr;
       return ukg_set_error(KALMAN_GPU_ENOMEM, "page-locked first-step table");
     }
     c.idx_cap = (size_t)std::max(T, 1);
   }
   for (int t = 0; t < T; ++t) c.idx[t] = p->track_start[t + 1] > p->track_start[t] ? p->track_start[t] : -1;
   char* B = (char*)c.dev;
-  int64_t* first = (int64_t*)(B + off[5]);
-  cudaMemcpyAsync(first, c.idx, (size_t)std::max(T, 1) * 8, cudaMemcpyHostToDevice, st);
+  const int64_t* first = c.idx_dev;
   double *G = (double*)(B + off[0]), *o = (double*)(B + off[1]), *C = (double*)(B + off[2]);
   char* ct = (char*)(B + off[3]);
   int32_t* rows = (int32_t*)(B + off[4]);

@@ -1855,6 +1855,167 @@ __global__ void __launch_bounds__(BS ? BS : 1024) solve_kernel(Args<T, T> a, int
 }
 
 /* ---------------------------------------------------------------------------
+ * back-substitution with covariances, register-tiled (n = 4, 6)
+ *
+ * The same arithmetic as solve_kernel with want_cov, in the same order (the
+ * results are equal bit for bit), but R, the reciprocals of its diagonal and
+ * the n x n accumulator M live in registers; only F~ and Y (2 n^2 entries) use
+ * the thread's shared-memory slice.  solve_kernel's slices (4 n^2 + 4 n
+ * entries) hold four warps per SM; here about ten fit, which the FP64 pipe and
+ * the double-float arithmetic both need to hide their latencies.
+ * ------------------------------------------------------------------------ */
+template <typename T, int N, int BS>
+__global__ void __launch_bounds__(BS) solve_cov_reg_kernel(Args<T, T> a)
+{
+  extern __shared__ unsigned char smem_raw[];
+  T* smem = reinterpret_cast<T*>(smem_raw);
+  const int64_t item = (int64_t)blockIdx.x * BS + threadIdx.x;
+  if (item >= a.ct.nsolve) return;
+  constexpr int nn = N * N;
+  const Rec<T>& Rr = a.cr;
+  const int t = find_track(a.ct.solve, a.ntracks, item);
+  const int64_t e = item - a.ct.solve[t];
+  const int64_t j = 2 * e, L = a.ct.L[t];
+  const bool hp = j > 0, hn = j + 1 < L;
+  const int64_t se = item;
+  const int64_t oj = orig_step(a.track_start, a.level, t, j);
+  const int64_t om = hp ? orig_step(a.track_start, a.level, t, j - 1) : 0;
+  const int64_t op = hn ? orig_step(a.track_start, a.level, t, j + 1) : 0;
+  PVc<T, BS> Fs{smem + threadIdx.x}, Ys = Fs + nn;
+  T R[N][N], dv[N];
+  bool bad = false;
+#pragma unroll
+  for (int c = 0; c < N; ++c)
+#pragma unroll
+    for (int i = 0; i <= c; ++i) R[i][c] = Rr.R.at(c * N + i, se);
+  for (int k = 0; k < nn; ++k) {
+    Fs[k] = hp ? Rr.Ft.at(k, se) : T(0);
+    Ys[k] = hn ? Rr.Y.at(k, se) : T(0);
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    bad |= (R[i][i] == T(0));
+    dv[i] = T(1) / R[i][i];
+  }
+  /* x <- R^{-1} x, the order of solve_upper */
+  auto solve = [&](T (&x)[N]) {
+#pragma unroll
+    for (int jj = N - 1; jj >= 0; --jj) {
+      const T xj = x[jj] * dv[jj];
+      x[jj] = xj;
+#pragma unroll
+      for (int i = 0; i < jj; ++i) x[i] = fma(-xj, R[i][jj], x[i]);
+    }
+  };
+
+  /* state */
+  T pv[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) pv[i] = a.yrhs.p ? a.yrhs.at(i, se) : Rr.rhs.at(i, se);
+  if (hp) {
+    const double* xm = a.state + om * N;
+    for (int k = 0; k < N; ++k) {
+      const T xk = ukg_df::narrow<T>(xm[k]);
+#pragma unroll
+      for (int i = 0; i < N; ++i) pv[i] = fma(-Fs[k * N + i], xk, pv[i]);
+    }
+  }
+  if (hn) {
+    const double* xp = a.state + op * N;
+    for (int k = 0; k < N; ++k) {
+      const T xk = ukg_df::narrow<T>(xp[k]);
+#pragma unroll
+      for (int i = 0; i < N; ++i) pv[i] = fma(-Ys[k * N + i], xk, pv[i]);
+    }
+  }
+  solve(pv);
+  double* xo = a.state + oj * N;
+#pragma unroll
+  for (int i = 0; i < N; ++i) xo[i] = ukg_df::widen(pv[i]);
+
+  const double* Smm = hp ? a.cov + om * nn : nullptr;
+  const double* Spp = hn ? a.cov + op * nn : nullptr;
+  const int64_t smp = (hp && hn) ? a.nt.slot[t] + (j + 1) / 2 : 0; /* U of the next level */
+  T M[N][N]; /* M[c][i]: column c, row i */
+#pragma unroll
+  for (int c = 0; c < N; ++c)
+#pragma unroll
+    for (int i = 0; i < N; ++i) M[c][i] = T(0);
+  const int q0 = hp ? 0 : N, q1 = hn ? 2 * N : N;
+#pragma unroll 1
+  for (int q = q0; q < q1; ++q) {
+    T sg[2 * N];
+    if (q < N) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) sg[i] = ukg_df::narrow<T>(Smm[(int64_t)q * N + i]);
+#pragma unroll
+      for (int i = 0; i < N; ++i) sg[N + i] = hn ? a.nr.U.at(i * N + q, smp) : T(0); /* Smp[q, :] */
+    } else {
+      const int qq = q - N;
+#pragma unroll
+      for (int i = 0; i < N; ++i) sg[i] = hp ? a.nr.U.at(qq * N + i, smp) : T(0);
+#pragma unroll
+      for (int i = 0; i < N; ++i) sg[N + i] = ukg_df::narrow<T>(Spp[(int64_t)qq * N + i]);
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) pv[i] = T(0);
+    if (hp)
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        const T sk = sg[k];
+#pragma unroll
+        for (int i = 0; i < N; ++i) pv[i] = fma(Fs[k * N + i], sk, pv[i]);
+      }
+    if (hn)
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        const T sk = sg[N + k];
+#pragma unroll
+        for (int i = 0; i < N; ++i) pv[i] = fma(Ys[k * N + i], sk, pv[i]);
+      }
+    PVc<T, BS> bq = q < N ? Fs + q * N : Ys + (q - N) * N; /* column q of B = [F~ | Y] */
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      const T bc = bq[c];
+#pragma unroll
+      for (int i = 0; i < N; ++i) M[c][i] = fma(pv[i], bc, M[c][i]);
+    }
+    if (a.level == 0) continue; /* level 0's off-diagonal blocks are not needed */
+    solve(pv);
+    if (q < N) { /* cov(x_{j-1}, x_j) = cov(x_j, x_{j-1})^T: row q */
+      const int64_t sU = a.ct.slot[t] + j;
+#pragma unroll
+      for (int i = 0; i < N; ++i) Rr.U.at(i * N + q, sU) = -pv[i];
+    } else {
+      const int64_t sU = a.ct.slot[t] + j + 1;
+#pragma unroll
+      for (int i = 0; i < N; ++i) Rr.U.at((q - N) * N + i, sU) = -pv[i];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) M[i][i] += T(1);
+  /* S = R^{-1} M R^{-T}: solve the columns, transpose, solve again, transpose */
+#pragma unroll
+  for (int c = 0; c < N; ++c) solve(M[c]);
+#pragma unroll
+  for (int c = 0; c < N; ++c)
+#pragma unroll
+    for (int i = c + 1; i < N; ++i) {
+      const T tmp = M[c][i];
+      M[c][i] = M[i][c];
+      M[i][c] = tmp;
+    }
+#pragma unroll
+  for (int c = 0; c < N; ++c) solve(M[c]);
+  double* So = a.cov + oj * nn;
+#pragma unroll
+  for (int c = 0; c < N; ++c)
+#pragma unroll
+    for (int i = 0; i < N; ++i) So[(int64_t)c * N + i] = ukg_df::widen(M[i][c]);
+  if (bad) atomicOr(a.flag, 2);
+}
+
+/* ---------------------------------------------------------------------------
  * refinement sweep kernels (FP32 factors, FP64 residual)
  * ------------------------------------------------------------------------ */
 
@@ -2484,6 +2645,7 @@ template <typename T>
 struct Kernels {
   void (*pair)(Args<T, T>, int) = nullptr;
   void (*solve)(Args<T, T>, int) = nullptr;
+  void (*solve_cov)(Args<T, T>) = nullptr; /* register-tiled back-substitution with covariances */
   int bp = 0, bs = 0;     /* fixed block sizes of the specialised kernels (0: pick) */
   size_t pair_smem = 0;   /* dynamic shared memory of the pair kernel (0: per-thread workspace) */
 };
@@ -2508,16 +2670,18 @@ Kernels<T> choose_kernels(int n, int mx, int pair_bp = kPairSsBP)
   if (n == mx && n == 6) {
     k.pair = pair_kernel<T, T, 6, 6, 128>;
     k.solve = solve_kernel<T, 6, 64>;
+    if constexpr (sizeof(T) != sizeof(float)) k.solve_cov = solve_cov_reg_kernel<T, 6, 64>;
     k.bp = 128;
     k.bs = 64;
   } else if (n == mx && n == 4) {
     k.pair = pair_kernel<T, T, 4, 4, 128>;
     k.solve = solve_kernel<T, 4, 64>;
+    if constexpr (sizeof(T) != sizeof(float)) k.solve_cov = solve_cov_reg_kernel<T, 4, 64>;
     k.bp = 128;
     k.bs = 64;
   } else if (n == mx && n == 8) {
     k.pair = pair_kernel<T, T, 8, 8, 128>;
-    k.solve = solve_kernel<T, 8, 64>;
+    k.solve = solve_kernel<T, 8, 64>; /* the register-tiled form spills at n = 8 */
     k.bp = 128;
     k.bs = 64;
   } else {
@@ -2732,6 +2896,12 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
         UKG_LAUNCH(kSolve, st, (RS.solve<<<grid(lp[l].nsolve, 128), 128, 0, st>>>(a)));
         continue;
       }
+    }
+    if (want_cov && K.solve_cov) {
+      const size_t smem_cov = (size_t)64 * 2 * nn * ts;
+      ukg_allow_dynamic_smem((const void*)K.solve_cov);
+      UKG_LAUNCH(kSolve, st, (K.solve_cov<<<grid(lp[l].nsolve, 64), 64, smem_cov, st>>>(a)));
+      continue;
     }
     UKG_LAUNCH(kSolve, st, (K.solve<<<grid(lp[l].nsolve, bs), bs, bs * pt_solve, st>>>(a, want_cov ? 1 : 0)));
   }

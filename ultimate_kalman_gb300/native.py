@@ -423,6 +423,7 @@ class Plan:
         if self.h:
             load().kalman_gpu_plan_destroy(self.h)
             self.h = None
+        self.owner = None  # the device arrays may be freed now
 
     def __del__(self):
         try:
