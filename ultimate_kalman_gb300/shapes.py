@@ -110,6 +110,9 @@ def main():
     ap.add_argument("--log-cov", action="store_true", help="covariance eigenvalues log-uniform in [1e-3, 1]")
     ap.add_argument("--device-build", action="store_true",
                     help="build the track on the GPU with the equation builder (no host copy of the equations)")
+    ap.add_argument("--batched", type=int, default=0, metavar="TRACKS",
+                    help="instead of one track: the first TRACKS of the batched workload (constant-velocity, n=6, "
+                         "m=3, lengths log-uniform in [100, 20000]); a small case of the same kernels for profiling")
     ap.add_argument("--time-build", action="store_true",
                     help="time the equation builder on the track (CUDA events) instead of smoothing it")
     args = ap.parse_args()
@@ -130,8 +133,12 @@ def main():
         return
     lo = 1e-3 if args.log_cov else 0.1
     rho = 0.995 if args.n >= 128 else 0.99
-    cov = not args.no_covariance and not args.fp32_refine
-    if args.device_build:
+    cov = not args.no_covariance and not (args.fp32_refine and args.batched == 0)
+    if args.batched:
+        P = pb.constant_velocity(pb.batched_lengths(4096, 100, 20000, seed=0)[:args.batched], seed=1000)
+        D = native.DeviceProblem(P, covariance=True)
+        args.k, args.n, args.m = int(P.nsteps), 6, 3
+    elif args.device_build:
         D = device_track(args.k, args.n, args.m, rho=rho, lo=lo, log_cov=args.log_cov, covariance=cov)
     else:
         P = synthetic_track(args.k, args.n, args.m, lo=lo, log_cov=args.log_cov, rho=rho)
