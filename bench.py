@@ -576,20 +576,16 @@ def large_state(stream):
     """The large-state shape beside the headline: one n=128, m=64, k=20,000
     track (F = 0.995 Q, G ~ N(0, 1/m), noise covariance eigenvalues
     log-uniform in [1e-3, 1], 5 % of steps unobserved), odd-even smoother,
-    states: the precision form (FP32 blocked QR + one FP64-residual sweep),
-    the same with 3xTF32 tensor-core updates, and plain FP64."""
+    states: the precision form (FP32 blocked QR + one FP64-residual sweep)
+    and plain FP64."""
     import torch
     from ultimate_kalman_gb300 import native, shapes
     P = shapes.synthetic_track(20000, 128, 64, rho=0.995, lo=1e-3, log_cov=True)
     D = native.DeviceProblem(P, covariance=False)
     kw32 = dict(covariance=False, fp32_refine=True, sweeps=1)
-    kwtc = dict(kw32, tf32x3=True)
     D.smooth("oddeven", **kw32)
     ms32, _ = time_smooths(D, 3, stream, **kw32)
     X32 = D.state.clone()
-    D.smooth("oddeven", **kwtc)
-    mstc, _ = time_smooths(D, 2, stream, **kwtc)
-    Xtc = D.state.clone()
     D.smooth("oddeven", covariance=False)
     ms64, _ = time_smooths(D, 2, stream, covariance=False)
     X64 = D.state
@@ -598,8 +594,6 @@ def large_state(stream):
                    "covariance eigenvalues log-uniform in [1e-3, 1], 5 % of steps unobserved; synthetic",
            "fp32_refine": {"ms": ms32, "steps_per_s": P.nsteps / (ms32 * 1e-3), "rel_err_vs_fp64": rel(X32),
                            "form": "FP32 blocked QR (FMA updates) + 1 FP64-residual sweep"},
-           "tf32x3": {"ms": mstc, "steps_per_s": P.nsteps / (mstc * 1e-3), "rel_err_vs_fp64": rel(Xtc),
-                      "form": "FP32 blocked QR, 3xTF32 tensor-core updates + 1 FP64-residual sweep"},
            "plain_fp64": {"ms": ms64, "steps_per_s": P.nsteps / (ms64 * 1e-3)},
            "speedup_fp32_refine_vs_fp64": ms64 / ms32}
     del D

@@ -58,10 +58,6 @@ enum {
 /* Number of refinement sweeps with KALMAN_GPU_FP32_REFINE (1..3; 0 selects the
  * default, 2).  Each sweep multiplies the error by about eps32 * cond(A)^2.  */
 #define KALMAN_GPU_REFINE_SWEEPS(k) (((uint32_t)(k) & 3u) << 21)
-/* With KALMAN_GPU_FP32_REFINE, at state dimensions 64..128: the blocked QR's
- * trailing updates run on the tensor cores in 3xTF32 (split TF32 products,
- * FP32 accumulation) instead of FP32 FMAs.  No reference counterpart.       */
-#define KALMAN_GPU_TF32X3 (1u << 23)
 
 /* Last error of the calling thread: status code and a one-line message.     */
 int         kalman_gpu_last_status(void);
@@ -209,8 +205,8 @@ double  kalman_gpu_measure_fp32_tflops(void);
  * that overlapped a call on the GPU would race on it.  Every call blocks the
  * host until its kernels have finished: it synchronizes the stream to read the
  * status.  It runs the plain FP64 smoother (per-thread kernels at every state
- * dimension up to the scratch limit); KALMAN_GPU_FP32_REFINE and
- * KALMAN_GPU_TF32X3 are refused with KALMAN_GPU_EINVAL.                      */
+ * dimension up to the scratch limit); KALMAN_GPU_FP32_REFINE is refused with
+ * KALMAN_GPU_EINVAL.                                                         */
 #define KALMAN_GPU_NOALLOC_SCRATCH_BYTES (64u << 20)
 int kalman_gpu_smooth_oddeven_noalloc(uint32_t options, const kalman_gpu_problem_t* p, void* cuda_stream);
 

@@ -73,16 +73,14 @@ def test_precision_form_larger_states(n, k):
 
 
 @pytest.mark.parametrize("n,k", [(64, 41), (96, 23), (128, 17)])
-def test_precision_form_tensor_core_updates(n, k):
-    """KALMAN_GPU_TF32X3: the blocked QR's trailing updates in 3xTF32 on the
-    tensor cores (64 <= n <= 128); after the FP64 refinement the states are
-    within 1e-9 of the oracle, like the FP32-FMA form."""
+def test_precision_form_blocked_qr(n, k):
+    """64 <= n <= 128: the FP32 blocked QR (panels of 16 reflectors, trailing
+    updates from their Gram matrix); after the FP64 refinement the states are
+    within 1e-9 of the oracle."""
     P = pb.random_dynamics([k, 5, 2], n, n // 2, seed=70 + n, per_step=True, missing=0.1)
-    X, _ = native.smooth(P, covariance=False, fp32_refine=True, tf32x3=True)
     X32, _ = native.smooth(P, covariance=False, fp32_refine=True)
     st, Xo, _ = oracle.smooth(P, "oddeven", covariance=False)
     assert st == 0
-    assert oracle.rel_err_states(X, Xo) < 1e-9
     assert oracle.rel_err_states(X32, Xo) < 1e-9
 
 

@@ -93,11 +93,10 @@ def test_larger_shapes_match_ordinary_entry_point_and_oracle(lib, n, m, lengths)
 def test_refuses_the_precision_form(lib):
     P = pb.constant_velocity([50], seed=6)
     D = native.DeviceProblem(P, covariance=False)
-    for extra in (native.KALMAN_GPU_FP32_REFINE, native.KALMAN_GPU_FP32_REFINE | native.KALMAN_GPU_TF32X3):
-        opts = native.options_for("oddeven", False) | extra
-        status, X, _ = run_noalloc(lib, D, covariance=False, opts=opts)
-        assert status == 1
-        assert "plain FP64" in native.last_error()[1]
+    opts = native.options_for("oddeven", False) | native.KALMAN_GPU_FP32_REFINE
+    status, X, _ = run_noalloc(lib, D, covariance=False, opts=opts)
+    assert status == 1
+    assert "plain FP64" in native.last_error()[1]
 
 
 def test_refuses_problems_beyond_the_scratch_array(lib):

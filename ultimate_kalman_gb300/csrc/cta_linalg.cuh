@@ -102,207 +102,6 @@ static __device__ void householder(T* A, int ld, int rows, int npiv, int cols, T
 constexpr int kWyNB = 16;
 constexpr int kWyRows = 8; /* trailing-column rows loaded together */
 
-/* ---- FP32 trailing update on the tensor cores (3xTF32) ----------------------
- * mma.sync m16n8k8 TF32 with FP32 accumulation.  Each FP32 operand x is split
- * into x_hi = tf32(x) and x_lo = tf32(x - x_hi); a product is accumulated as
- * a_lo b_hi + a_hi b_lo + a_hi b_hi (the 3xTF32 scheme: about FP32 accuracy,
- * the a_lo b_lo term dropped).  Fragment layouts (PTX ISA, m16n8k8 .tf32):
- * g = lane / 4, q = lane % 4; A (16 x 8, row) a0 (g, q) a1 (g+8, q)
- * a2 (g, q+4) a3 (g+8, q+4); B (8 x 8, col) b0 (q, g) b1 (q+4, g);
- * D (16 x 8) d0 (g, 2q) d1 (g, 2q+1) d2 (g+8, 2q) d3 (g+8, 2q+1).           */
-static __device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo)
-{
-  uint32_t h, l;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
-  const float r = x - __uint_as_float(h);
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(r));
-  hi = h;
-  lo = l;
-}
-static __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
-{
-  asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-               "{%0,%1,%2,%3};"
-               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-/* d += a b in 3xTF32 from split fragments: the small terms first */
-static __device__ __forceinline__ void mma3(float (&d)[4], const uint32_t (&ah)[4], const uint32_t (&al)[4],
-                                            uint32_t bh0, uint32_t bl0, uint32_t bh1, uint32_t bl1)
-{
-  mma_tf32(d, al, bh0, bh1);
-  mma_tf32(d, ah, bl0, bl1);
-  mma_tf32(d, ah, bh0, bh1);
-}
-static __device__ __forceinline__ void split4(const float (&a)[4], uint32_t (&h)[4], uint32_t (&l)[4])
-{
-#pragma unroll
-  for (int r = 0; r < 4; ++r) split_tf32(a[r], h[r], l[r]);
-}
-
-/* Applies the panel's reflectors to the trailing columns c0..cols-1 of the
- * row-major C (rows 0..prow-1), as wy_columns does, with every product on the
- * tensor cores.  Warp 0 first forms the compact-WY factor T (LAPACK dlarft,
- * forward columnwise: T(j, j) = tau_j, T(0:j, j) = -tau_j T(0:j, 0:j) G(0:j, j),
- * so that H_{kb-1} .. H_0 = I - V T^T V^T).  Then each warp takes tiles of
- * 16 columns: W = C_tile^T V (K = rows in k-steps of 8), U = W T, and
- * C_tile -= (V U^T) over row tiles of 8.  V (unit form) and G are in shared
- * memory; T, W and U go through shared memory between the products.        */
-constexpr int kTcSteps = 4; /* k-steps (row tiles) of 8 rows per batch */
-static __device__ void wy_tiles_tf32x3(float* C, int ld, int prow, int c0, int cols, const float* Vs, const float* Gs,
-                                       const float* taus, int kb)
-{
-  __shared__ float Ws[NT / 32][16][17];
-  __shared__ float Tm[16][17];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
-  if (warp == 0) { /* T, column by column; lane i owns row i */
-    const int i = lane;
-    for (int j = 0; j < 16; ++j) {
-      float t = 0.f;
-      if (i < 16 && j < kb) {
-        if (i == j) t = taus[j];
-        else if (i < j) {
-          float sm = 0.f;
-          for (int l = i; l < j; ++l) sm = fmaf(Tm[i][l], Gs[l * 16 + j], sm);
-          t = -taus[j] * sm;
-        }
-      }
-      if (i < 16) Tm[i][j] = t;
-      __syncwarp();
-    }
-  }
-  __syncthreads();
-  /* T as the B operand of U = W T (K = l, N = b), split once */
-  uint32_t th[2][2][2], tl[2][2][2]; /* [k-step][n-tile][b0/b1] */
-#pragma unroll
-  for (int kk = 0; kk < 2; ++kk)
-#pragma unroll
-    for (int nt = 0; nt < 2; ++nt) {
-      split_tf32(Tm[kk * 8 + q][nt * 8 + g], th[kk][nt][0], tl[kk][nt][0]);
-      split_tf32(Tm[kk * 8 + q + 4][nt * 8 + g], th[kk][nt][1], tl[kk][nt][1]);
-    }
-  float(*W)[17] = Ws[warp];
-  const int ntiles = (cols - c0 + 15) / 16;
-  for (int tile = warp; tile < ntiles; tile += NT / 32) {
-    const int cb = c0 + 16 * tile;
-    const bool m0ok = cb + g < cols, m1ok = cb + g + 8 < cols;
-    /* W = C_tile^T V: M = 16 columns, N = 16 reflectors (two n-tiles), K = rows,
-       kTcSteps k-steps at a time (their loads in flight together, their
-       products into separate accumulators) */
-    float d[kTcSteps][2][4];
-#pragma unroll
-    for (int u = 0; u < kTcSteps; ++u)
-#pragma unroll
-      for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-        for (int r = 0; r < 4; ++r) d[u][nt][r] = 0.f;
-#pragma unroll 1
-    for (int i0 = 0; i0 < prow; i0 += 8 * kTcSteps) {
-      float a[kTcSteps][4];
-#pragma unroll
-      for (int u = 0; u < kTcSteps; ++u) {
-        const int r0 = i0 + 8 * u + q, r1 = r0 + 4;
-        const bool ok0 = r0 < prow, ok1 = r1 < prow;
-        a[u][0] = ok0 && m0ok ? C[(int64_t)r0 * ld + cb + g] : 0.f;
-        a[u][1] = ok0 && m1ok ? C[(int64_t)r0 * ld + cb + g + 8] : 0.f;
-        a[u][2] = ok1 && m0ok ? C[(int64_t)r1 * ld + cb + g] : 0.f;
-        a[u][3] = ok1 && m1ok ? C[(int64_t)r1 * ld + cb + g + 8] : 0.f;
-      }
-#pragma unroll
-      for (int u = 0; u < kTcSteps; ++u) {
-        const int r0 = i0 + 8 * u + q, r1 = r0 + 4;
-        const bool ok0 = r0 < prow, ok1 = r1 < prow;
-        uint32_t ah[4], al[4];
-        split4(a[u], ah, al);
-#pragma unroll
-        for (int nt = 0; nt < 2; ++nt) {
-          uint32_t bh0, bl0, bh1, bl1;
-          split_tf32(ok0 ? Vs[r0 * 16 + nt * 8 + g] : 0.f, bh0, bl0);
-          split_tf32(ok1 ? Vs[r1 * 16 + nt * 8 + g] : 0.f, bh1, bl1);
-          mma3(d[u][nt], ah, al, bh0, bl0, bh1, bl1);
-        }
-      }
-    }
-#pragma unroll
-    for (int u = 1; u < kTcSteps; ++u)
-#pragma unroll
-      for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-        for (int r = 0; r < 4; ++r) d[0][nt][r] += d[u][nt][r];
-#pragma unroll
-    for (int nt = 0; nt < 2; ++nt) {
-      W[g][nt * 8 + 2 * q] = d[0][nt][0];
-      W[g][nt * 8 + 2 * q + 1] = d[0][nt][1];
-      W[g + 8][nt * 8 + 2 * q] = d[0][nt][2];
-      W[g + 8][nt * 8 + 2 * q + 1] = d[0][nt][3];
-    }
-    __syncwarp();
-    /* U = W T: M = 16 columns, N = 16, K = 16 */
-    float uacc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-#pragma unroll
-    for (int kk = 0; kk < 2; ++kk) {
-      const float wa[4] = {W[g][kk * 8 + q], W[g + 8][kk * 8 + q], W[g][kk * 8 + q + 4], W[g + 8][kk * 8 + q + 4]};
-      uint32_t wh[4], wl[4];
-      split4(wa, wh, wl);
-#pragma unroll
-      for (int nt = 0; nt < 2; ++nt) mma3(uacc[nt], wh, wl, th[kk][nt][0], tl[kk][nt][0], th[kk][nt][1], tl[kk][nt][1]);
-    }
-    __syncwarp();
-#pragma unroll
-    for (int nt = 0; nt < 2; ++nt) {
-      W[g][nt * 8 + 2 * q] = uacc[nt][0];
-      W[g][nt * 8 + 2 * q + 1] = uacc[nt][1];
-      W[g + 8][nt * 8 + 2 * q] = uacc[nt][2];
-      W[g + 8][nt * 8 + 2 * q + 1] = uacc[nt][3];
-    }
-    __syncwarp();
-    /* C_tile -= U V^T: M = 16 columns, N = 8 rows per tile, K = 16 reflectors */
-    uint32_t uh[2][4], ul[2][4];
-#pragma unroll
-    for (int kk = 0; kk < 2; ++kk) {
-      const float ua[4] = {W[g][kk * 8 + q], W[g + 8][kk * 8 + q], W[g][kk * 8 + q + 4], W[g + 8][kk * 8 + q + 4]};
-      split4(ua, uh[kk], ul[kk]);
-    }
-#pragma unroll 1
-    for (int i0 = 0; i0 < prow; i0 += 8 * kTcSteps) {
-      /* the tiles' C entries first (in flight together), then the products */
-      float cv[kTcSteps][4];
-#pragma unroll
-      for (int u = 0; u < kTcSteps; ++u) {
-        const int ra = i0 + 8 * u + 2 * q, rc = ra + 1;
-        cv[u][0] = m0ok && ra < prow ? C[(int64_t)ra * ld + cb + g] : 0.f;
-        cv[u][1] = m0ok && rc < prow ? C[(int64_t)rc * ld + cb + g] : 0.f;
-        cv[u][2] = m1ok && ra < prow ? C[(int64_t)ra * ld + cb + g + 8] : 0.f;
-        cv[u][3] = m1ok && rc < prow ? C[(int64_t)rc * ld + cb + g + 8] : 0.f;
-      }
-#pragma unroll
-      for (int u = 0; u < kTcSteps; ++u) {
-        const int rb = i0 + 8 * u + g; /* this lane's B column: row rb of V */
-        const bool okb = rb < prow;
-        float e[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int kk = 0; kk < 2; ++kk) {
-          uint32_t bh0, bl0, bh1, bl1;
-          split_tf32(okb ? Vs[rb * 16 + kk * 8 + q] : 0.f, bh0, bl0);
-          split_tf32(okb ? Vs[rb * 16 + kk * 8 + q + 4] : 0.f, bh1, bl1);
-          mma3(e, uh[kk], ul[kk], bh0, bl0, bh1, bl1);
-        }
-        /* e: (column g, rows ra, ra+1), (column g+8, same rows) */
-        const int ra = i0 + 8 * u + 2 * q, rc = ra + 1;
-        if (m0ok) {
-          if (ra < prow) C[(int64_t)ra * ld + cb + g] = cv[u][0] - e[0];
-          if (rc < prow) C[(int64_t)rc * ld + cb + g] = cv[u][1] - e[1];
-        }
-        if (m1ok) {
-          if (ra < prow) C[(int64_t)ra * ld + cb + g + 8] = cv[u][2] - e[2];
-          if (rc < prow) C[(int64_t)rc * ld + cb + g + 8] = cv[u][3] - e[3];
-        }
-      }
-    }
-    __syncwarp();
-  }
-}
-
 /* shared-memory entries householder_wy works in: the panel (rows x kWyNB,
  * zero-padded), the reflectors' Gram matrix, their tau factors and column
  * scales, partial dot products (4 warps x kWyNB), look-ahead norms (4) */
@@ -393,7 +192,7 @@ static __device__ __forceinline__ void wy_columns(T* C, int ld, int prow, int c,
     }
 }
 
-template <bool kTensorCores, typename T>
+template <typename T>
 static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols, T* red, T* sh)
 {
   static_assert(NT == 8 * kWyNB, "the panel factorization maps the CTA to kWyNB columns x 8 row groups");
@@ -502,14 +301,10 @@ static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols
     }
     __syncthreads();
     T* C = A + (int64_t)k0 * ld; /* rows k0.. */
-    if constexpr (sizeof(T) == sizeof(float) && kTensorCores) {
-      wy_tiles_tf32x3(C, ld, prow, c0, cols, Vs, Gs, taus, kb);
-    } else {
-      int c = c0 + tid;
-      if constexpr (sizeof(T) == sizeof(float)) /* two columns per thread: twice the loads in flight */
-        for (; c + NT < cols; c += 2 * NT) wy_columns<2>(C, ld, prow, c, NT, Vs, Gs, taus, kb);
-      for (; c < cols; c += NT) wy_columns<1>(C, ld, prow, c, 0, Vs, Gs, taus, kb);
-    }
+    int c = c0 + tid;
+    if constexpr (sizeof(T) == sizeof(float)) /* two columns per thread: twice the loads in flight */
+      for (; c + NT < cols; c += 2 * NT) wy_columns<2>(C, ld, prow, c, NT, Vs, Gs, taus, kb);
+    for (; c < cols; c += NT) wy_columns<1>(C, ld, prow, c, 0, Vs, Gs, taus, kb);
     __syncthreads();
   }
 }
@@ -518,10 +313,10 @@ static __device__ void householder_wy(T* A, int ld, int rows, int npiv, int cols
  * states from 64 on instantiate the blocked form (at n = 128 the odd-even pair
  * kernel runs 2.3x faster with it), the others keep the unblocked form and
  * its small shared-memory footprint (at n = 48 the panels then stay in L1). */
-template <bool kBlocked, bool kTensorCores = false, typename T>
+template <bool kBlocked, typename T>
 static __device__ __forceinline__ void panel_qr(T* A, int ld, int rows, int npiv, int cols, T* red, T* sh)
 {
-  if (kBlocked && npiv >= kWyNB && cols > npiv) householder_wy<kTensorCores>(A, ld, rows, npiv, cols, red, sh);
+  if (kBlocked && npiv >= kWyNB && cols > npiv) householder_wy(A, ld, rows, npiv, cols, red, sh);
   else householder(A, ld, rows, npiv, cols, red);
 }
 constexpr int kBlockedMinN = 64;

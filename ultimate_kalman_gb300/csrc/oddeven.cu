@@ -3205,28 +3205,19 @@ int run_plan_cta(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t s
   }
   const int kPair = P.fp32 ? UKG_K_PAIR32 : kDD ? UKG_K_DF_PAIR : UKG_K_PAIR;
   const int kSolve = P.fp32 ? UKG_K_SOLVE32 : kDD ? UKG_K_DF_SOLVE : UKG_K_SOLVE;
-  /* 3xTF32 tensor-core trailing updates in the FP32 blocked QR (an option) */
-  constexpr bool kF32 = sizeof(T) == sizeof(float);
-  const bool tc = kF32 && (options & KALMAN_GPU_TF32X3) != 0;
   for (int l = 0; l < nlev; ++l) {
     ctak::CArgs<T> a;
     common(a, l);
     a.ce = eq_level(l);
     if (l + 1 < nlev) a.ne = eq_level(l + 1);
     if (lp[l].npairs > 0) {
-      if (n >= cta::kBlockedMinN && tc) {
-        if constexpr (kF32)
-          UKG_LAUNCH(kPair, st, (ctak::pair_cta<T, true, true><<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
-      } else if (n >= cta::kBlockedMinN)
+      if (n >= cta::kBlockedMinN)
         UKG_LAUNCH(kPair, st, (ctak::pair_cta<T, true><<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
       else
         UKG_LAUNCH(kPair, st, (ctak::pair_cta<T, false><<<grid(lp[l].npairs), cta::NT, 0, st>>>(a)));
     }
     if (lp[l].ntail > 0) {
-      if (n >= cta::kBlockedMinN && tc) {
-        if constexpr (kF32)
-          UKG_LAUNCH(UKG_K_TAIL, st, (ctak::tail_cta<T, true, true><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
-      } else if (n >= cta::kBlockedMinN)
+      if (n >= cta::kBlockedMinN)
         UKG_LAUNCH(kTail, st, (ctak::tail_cta<T, true><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
       else
         UKG_LAUNCH(kTail, st, (ctak::tail_cta<T, false><<<grid(lp[l].ntail), cta::NT, 0, st>>>(a)));
@@ -3462,9 +3453,9 @@ extern "C" int kalman_gpu_smooth_oddeven_noalloc(uint32_t options, const kalman_
   if (p->location != KALMAN_GPU_DEVICE)
     return ukg_set_error(KALMAN_GPU_EINVAL, "the allocation-free entry point takes device arrays only "
                          "(host arrays would need a device copy)");
-  if (options & (KALMAN_GPU_FP32_REFINE | KALMAN_GPU_TF32X3))
+  if (options & KALMAN_GPU_FP32_REFINE)
     return ukg_set_error(KALMAN_GPU_EINVAL, "the allocation-free entry point runs the plain FP64 smoother only "
-                         "(KALMAN_GPU_FP32_REFINE and KALMAN_GPU_TF32X3 are not accepted)");
+                         "(KALMAN_GPU_FP32_REFINE is not accepted)");
   if (p->nsteps == 0) return 0;
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
   int dev = 0;

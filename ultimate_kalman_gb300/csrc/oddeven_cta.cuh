@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(NT) weigh_cta(CArgs<T> a, RawA raw, int64_t ns
  * forward elimination of one pair per CTA: stages A, C, B
  * Scratch: the largest panel, 2n x (3n+1).
  * ------------------------------------------------------------------------ */
-template <typename T, bool kBlocked, bool kTc = false>
+template <typename T, bool kBlocked>
 __global__ void __launch_bounds__(NT, 4) pair_cta(CArgs<T> a)
 {
   __shared__ T red[33];
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(NT, 4) pair_cta(CArgs<T> a)
         A[e] = v;
       }
       __syncthreads();
-      ::cta::panel_qr<kBlocked, kTc>(A, ld, rows, n, ld, red, sh);
+      ::cta::panel_qr<kBlocked>(A, ld, rows, n, ld, red, sh);
       for (int e = tid; e < n * n; e += NT) {
         const int r = e / n, c = e - r * n; /* R~ (r, c), Y~ (r, c) */
         Rr.R.at(c * n + r, se) = r <= c ? A[(int64_t)r * ld + c] : T(0);
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(NT, 4) pair_cta(CArgs<T> a)
                       : (c < n ? C.G.at(c * mx + (r - mj), sj1) : C.o.at(r - mj, sj1));
       }
       __syncthreads();
-      ::cta::panel_qr<kBlocked, kTc>(A, ld, rows, n, ld, red, sh);
+      ::cta::panel_qr<kBlocked>(A, ld, rows, n, ld, red, sh);
       const int g2 = rows < n ? rows : n;
       for (int e = tid; e < g2 * n; e += NT) {
         const int r = e / n, c = e - r * n;
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(NT, 4) pair_cta(CArgs<T> a)
         A[e] = v;
       }
       __syncthreads();
-      ::cta::panel_qr<kBlocked, kTc>(A, ld, rows, n, ld, red, sh);
+      ::cta::panel_qr<kBlocked>(A, ld, rows, n, ld, red, sh);
       for (int e = tid; e < n * n; e += NT) {
         const int r = e / n, c = e - r * n;
         Rr.R.at(c * n + r, se) = r <= c ? A[(int64_t)r * ld + c] : T(0);
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(NT, 4) pair_cta(CArgs<T> a)
  * odd-length tracks: the single last step and its fix-up, or the base case.
  * Scratch: the (n+m) x (2n+1) panel, an n x n inverse, an n-vector.
  * ------------------------------------------------------------------------ */
-template <typename T, bool kBlocked, bool kTc = false>
+template <typename T, bool kBlocked>
 __global__ void __launch_bounds__(NT) tail_cta(CArgs<T> a)
 {
   __shared__ T red[33];
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs<T> a)
         A[e] = c < n ? C.G.at(c * mx + r, sb) : C.o.at(r, sb);
       }
       __syncthreads();
-      ::cta::panel_qr<kBlocked, kTc>(A, ld, m0, n, ld, red, sh);
+      ::cta::panel_qr<kBlocked>(A, ld, m0, n, ld, red, sh);
       if (tid == 0)
         for (int i = 0; i < n; ++i)
           if (A[(int64_t)i * ld + i] == T(0)) atomicOr(a.flag, 2);
@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs<T> a)
         WS[e] = c < n ? C.G.at(c * mx + r, s) : C.o.at(r, s);
       }
       __syncthreads();
-      ::cta::panel_qr<kBlocked, kTc>(WS, ldA, ms, n, ldA, red, sh);
+      ::cta::panel_qr<kBlocked>(WS, ldA, ms, n, ldA, red, sh);
     }
     for (int e = tid; e < rowsT * ldT; e += NT) {
       const int r = e / ldT, c = e - r * ldT;
@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs<T> a)
       WT[e] = v;
     }
     __syncthreads();
-    ::cta::panel_qr<kBlocked, kTc>(WT, ldT, rowsT, n, ldT, red, sh);
+    ::cta::panel_qr<kBlocked>(WT, ldT, rowsT, n, ldT, red, sh);
     for (int e = tid; e < n * n; e += NT) {
       const int r = e / n, c = e - r * n;
       Rr.R.at(c * n + r, es) = r <= c ? WT[(int64_t)r * ldT + c] : T(0);
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(NT) tail_cta(CArgs<T> a)
                      : (c < n ? WT[(int64_t)(n + r - gp) * ldT + n + c] : WT[(int64_t)(n + r - gp) * ldT + 2 * n]);
     }
     __syncthreads();
-    ::cta::panel_qr<kBlocked, kTc>(WF, ldF, rF, n, ldF, red, sh);
+    ::cta::panel_qr<kBlocked>(WF, ldF, rF, n, ldF, red, sh);
     const int g2 = rF < n ? rF : n;
     for (int e = tid; e < g2 * n; e += NT) {
       const int r = e / n, c = e - r * n;

@@ -29,7 +29,6 @@ KALMAN_ALGORITHM_ODDEVEN = 1 << 2
 KALMAN_ALGORITHM_ASSOCIATIVE = 1 << 3
 KALMAN_NO_COVARIANCE = 1 << 16
 KALMAN_GPU_FP32_REFINE = 1 << 20
-KALMAN_GPU_TF32X3 = 1 << 23
 KALMAN_GPU_DEVICE, KALMAN_GPU_HOST = 0, 1
 KALMAN_GPU_OK, KALMAN_GPU_EINVAL, KALMAN_GPU_ECUDA, KALMAN_GPU_ENOMEM, KALMAN_GPU_ESINGULAR, KALMAN_GPU_ENODEV = range(6)
 
@@ -303,14 +302,12 @@ def release():
     load().kalman_gpu_release()
 
 
-def options_for(algorithm, covariance=True, fp32_refine=False, sweeps=0, tf32x3=False):
+def options_for(algorithm, covariance=True, fp32_refine=False, sweeps=0):
     o = KALMAN_ALGORITHM_ODDEVEN if algorithm == "oddeven" else KALMAN_ALGORITHM_ASSOCIATIVE
     if not covariance:
         o |= KALMAN_NO_COVARIANCE
     if fp32_refine:
         o |= KALMAN_GPU_FP32_REFINE | ((sweeps & 3) << 21)
-        if tf32x3:
-            o |= KALMAN_GPU_TF32X3
     return o
 
 
@@ -359,12 +356,11 @@ class DeviceProblem:
     def input_bytes(self):
         return sum(a.numel() * a.element_size() for a in self.arrays.values())
 
-    def smooth(self, algorithm="oddeven", covariance=True, fp32_refine=False, stream=None, check=True, sweeps=0,
-               tf32x3=False):
+    def smooth(self, algorithm="oddeven", covariance=True, fp32_refine=False, stream=None, check=True, sweeps=0):
         L = load()
         torch = self.torch
         st = stream if stream is not None else torch.cuda.current_stream()
-        opts = options_for(algorithm, covariance and self.cov is not None, fp32_refine, sweeps, tf32x3)
+        opts = options_for(algorithm, covariance and self.cov is not None, fp32_refine, sweeps)
         f = L.kalman_gpu_smooth_oddeven_packed if algorithm == "oddeven" else L.kalman_gpu_smooth_associative_packed
         status = f(opts, ctypes.byref(self.struct), ctypes.c_void_p(st.cuda_stream))
         if check:
@@ -432,13 +428,13 @@ class Plan:
             pass
 
 
-def smooth(P, algorithm="oddeven", covariance=True, fp32_refine=False, location="device", sweeps=0, tf32x3=False):
+def smooth(P, algorithm="oddeven", covariance=True, fp32_refine=False, location="device", sweeps=0):
     """Smooths a PackedProblem on the GPU; returns (states [N,n], covs [N,n,n] or None).
     location="device": inputs are copied to GPU memory first and the device
     entry point runs on them; "host": the library is handed host arrays."""
     if location == "device":
         D = DeviceProblem(P, covariance)
-        D.smooth(algorithm, covariance, fp32_refine, sweeps=sweeps, tf32x3=tf32x3)
+        D.smooth(algorithm, covariance, fp32_refine, sweeps=sweeps)
         return D.results()
     L = load()
     N, n = P.nsteps, P.n
@@ -454,7 +450,7 @@ def smooth(P, algorithm="oddeven", covariance=True, fp32_refine=False, location=
         setattr(s, f, arrs[f].ctypes.data)
     s.state = state.ctypes.data
     s.covariance = cov.ctypes.data if cov is not None else None
-    opts = options_for(algorithm, covariance, fp32_refine, sweeps, tf32x3)
+    opts = options_for(algorithm, covariance, fp32_refine, sweeps)
     f = L.kalman_gpu_smooth_oddeven_packed if algorithm == "oddeven" else L.kalman_gpu_smooth_associative_packed
     _check(f(opts, ctypes.byref(s), None))
     if cov is not None:

@@ -198,12 +198,13 @@ def constant_velocity(lengths, seed=0, K_type="C", C_type="C", missing=0.0, fold
 def _set_cov(arr, types, s, dim, cov, kind):
     """Stores the covariance `cov` (dim x dim) for steps s in the factor form
     `kind` ('C' explicit, 'W' inverse square-root factor, 'w' inverse std
-    column, 'F' lower Cholesky factor)."""
+    column, 'F' and 'U' lower Cholesky factor -- the reference weighs both
+    kinds with the lower triangle, c/kalman_base.c)."""
     if len(s) == 0:
         return
     if kind == "C":
         arr[s, :dim, :dim] = cov.T
-    elif kind == "F":
+    elif kind in ("F", "U"):
         arr[s, :dim, :dim] = np.linalg.cholesky(cov).T
     elif kind == "W":
         w, V = np.linalg.eigh(cov)

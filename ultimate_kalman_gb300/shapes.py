@@ -105,7 +105,6 @@ def main():
     ap.add_argument("--no-covariance", action="store_true")
     ap.add_argument("--fp32-refine", action="store_true", help="the precision form (odd-even; states)")
     ap.add_argument("--sweeps", type=int, default=0)
-    ap.add_argument("--tf32x3", action="store_true", help="precision form: 3xTF32 tensor-core QR updates (n >= 64)")
     ap.add_argument("--repeats", type=int, default=3)
     ap.add_argument("--log-cov", action="store_true", help="covariance eigenvalues log-uniform in [1e-3, 1]")
     ap.add_argument("--device-build", action="store_true",
@@ -143,7 +142,7 @@ def main():
     else:
         P = synthetic_track(args.k, args.n, args.m, lo=lo, log_cov=args.log_cov, rho=rho)
         D = native.DeviceProblem(P, covariance=True)
-    kw = dict(covariance=cov, fp32_refine=args.fp32_refine, sweeps=args.sweeps, tf32x3=args.tf32x3)
+    kw = dict(covariance=cov, fp32_refine=args.fp32_refine, sweeps=args.sweeps)
     D.smooth(args.algorithm, **kw)
     torch.cuda.synchronize()
     native.profile_enable(True)
@@ -163,7 +162,7 @@ def main():
         X64 = D.state
         rel_err = float(((X32 - X64).abs().amax(dim=1) / X64.abs().amax(dim=1)).max().item())
     print(json.dumps({"algorithm": args.algorithm, "n": args.n, "m": args.m, "k": args.k, "covariance": cov,
-                      "fp32_refine": args.fp32_refine, "tf32x3": args.tf32x3, "rel_err_vs_fp64": rel_err,
+                      "fp32_refine": args.fp32_refine, "rel_err_vs_fp64": rel_err,
                       "ms": ms, "steps_per_s": args.k / (ms * 1e-3),
                       "per_kernel_ms": {k2: v[0] / args.repeats for k2, v in prof.items()},
                       "input_gb": D.input_bytes() / 1e9}))
