@@ -126,12 +126,18 @@ def test_unobservable_reports_singular():
     assert e.value.status == 4
 
 
-def test_malformed_observation_rows_on_device():
-    P = pb.constant_velocity([6], seed=1)
+@pytest.mark.parametrize("location", ["device", "host"])
+@pytest.mark.parametrize("fp32_refine", [False, True])
+def test_malformed_observation_rows(location, fp32_refine):
+    """Observation rows outside [0, mmax] are reported as malformed input by
+    the kernels that read them, for device and host arrays."""
+    P = pb.constant_velocity([6, 40], seed=1)
     P.obs_rows[2] = P.mmax + 3
+    P.obs_rows[20] = -1
     with pytest.raises(native.KalmanError) as e:
-        native.smooth(P, location="device")
+        native.smooth(P, location=location, covariance=not fp32_refine, fp32_refine=fp32_refine)
     assert e.value.status == 1
+    assert "malformed input" in native.last_error()[1]
 
 
 @pytest.mark.parametrize("n,k", [(9, 41), (12, 300), (24, 120), (48, 40)])
