@@ -383,7 +383,7 @@ def run_gpu(args):
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 factorization + f64 residual refinement", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f32 factorization + double-float (f32 pair, ~47-bit) residual refinement; f64 in and out", "data": "synthetic",
             "config": config_dict(P, args.tracks, world), "gpu_launches": int(launches),
             "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
                            "what": "one smoothing of all 4,096 tracks"},

@@ -174,7 +174,11 @@ def test_served_results_equal_results_alone(fp32):
 def test_two_batches_in_flight_overlap_on_the_device_and_match_alone():
     """Requests of two shape classes arrive together; with two lanes both
     batches are on the GPU at once (their device intervals intersect) and every
-    result equals the request smoothed alone, bit for bit."""
+    result equals the request smoothed alone, bit for bit.  Each batch holds one
+    request (max_batch_steps below two requests' steps), so a batch needs no
+    device-side concatenation before its start is recorded: the interval
+    starts when the lane's stream reaches the smoothing, not when a copy
+    kernel queued behind the other lane's kernels gets an SM."""
     import torch
     if not torch.cuda.is_available():
         pytest.skip("needs a CUDA device")
@@ -185,7 +189,7 @@ def test_two_batches_in_flight_overlap_on_the_device_and_match_alone():
     for _ in range(2):  # the first pass warms the lanes (workspaces, kernel loading), the second is checked
         reqs = [serve.Request(i, 0.0, P, covariance=(P.n == 6)) for i, P in enumerate(problems)]
         ex.intervals.clear()
-        srv = serve.Server(ex, hbm_budget=1 << 36, max_batch_steps=80000)
+        srv = serve.Server(ex, hbm_budget=1 << 36, max_batch_steps=60000)
         done = srv.serve(reqs)
     ex.close()
     assert srv.max_running == 2
