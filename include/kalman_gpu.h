@@ -189,6 +189,15 @@ int64_t kalman_gpu_launch_count(void);
 double  kalman_gpu_measure_fp64_tflops(int active_lanes);
 /* The same for FP32 fused multiply-adds (all lanes active).                 */
 double  kalman_gpu_measure_fp32_tflops(void);
+/* Checks the device-side failure path of the library's bounded waits: one
+ * thread block arms an mbarrier for a transfer that nothing delivers, waits
+ * with the same bound as the kernels' waits on their bulk copies (about a
+ * second), and reports the outcome through the same error flag.  Returns
+ * KALMAN_GPU_ECUDA with the message of a copy that did not complete in time
+ * (the expected outcome), KALMAN_GPU_OK if the wait was satisfied, or the
+ * status of a CUDA error.  No asynchronous copy is in flight when the block
+ * exits.  A diagnostic; takes about a second.                               */
+int     kalman_gpu_check_bounded_wait(void* cuda_stream);
 
 /* Allocation-free odd-even smoothing of a packed problem held in DEVICE
  * memory.  No counterpart in the reference: it exists for callers that must

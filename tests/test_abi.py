@@ -62,6 +62,7 @@ def test_no_device_is_reported_not_fatal(lib):
     assert e.value.status == 5
     X, S, status = native.smooth_equations(P)
     assert status == 5 and np.isnan(X).all() and np.isnan(S).all()
+    assert lib.kalman_gpu_check_bounded_wait(None) == native.KALMAN_GPU_ENODEV
 
 
 def _mat(lib, A, keep):

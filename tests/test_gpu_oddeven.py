@@ -126,6 +126,22 @@ def test_unobservable_reports_singular():
     assert e.value.status == 4
 
 
+def test_bounded_wait_gives_up_and_the_context_stays_usable():
+    """The device side of a bounded wait that runs out (an mbarrier armed for
+    a transfer nothing delivers): the kernel gives up after its bound, the host
+    reads the error flag and reports ECUDA, and the next smoothing on the same
+    context is correct."""
+    import time
+    L = native.load()
+    t0 = time.perf_counter()
+    assert L.kalman_gpu_check_bounded_wait(None) == native.KALMAN_GPU_ECUDA
+    assert "did not complete in time" in native.last_error()[1]
+    assert time.perf_counter() - t0 < 30.0
+    P = pb.constant_velocity([300, 7], seed=8)
+    X, S = native.smooth(P)
+    check(P, X, S)
+
+
 @pytest.mark.parametrize("location", ["device", "host"])
 @pytest.mark.parametrize("fp32_refine", [False, True])
 def test_malformed_observation_rows(location, fp32_refine):

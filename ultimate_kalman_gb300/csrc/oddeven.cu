@@ -413,6 +413,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
   return false;
 }
 
+/* the failure path of mbar_wait (kalman_gpu_check_bounded_wait): an mbarrier
+ * armed for 16 bytes that no copy delivers never completes its phase; the
+ * bounded wait gives up and the block reports flag bit 8, as the weighing
+ * kernels do.  No copy is issued, so none is in flight when the block exits. */
+__global__ void bounded_wait_check_kernel(int* flag)
+{
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&bar)), "r"(16u) : "memory");
+    if (!mbar_wait(&bar, 0)) atomicOr(flag, 8);
+  }
+}
+
 /* prepared weighing of one covariance factor in per-thread shared memory:
  * 'C' Cholesky factor, 'U'/'F' lower triangle (L and reciprocal diagonal),
  * 'W' the matrix itself (in L), 'w' the column (in dinv)                     */
@@ -3368,6 +3382,30 @@ extern "C" int ukg_oddeven_device(uint32_t options, const kalman_gpu_problem_t* 
  * these options (the workspace of ukg_oddeven_device, with its 1/8 slack):
  * a caller that budgets HBM (the serving loop) reads the library's own
  * figure instead of modelling it.  -1 on a malformed problem.              */
+extern "C" int kalman_gpu_check_bounded_wait(void* cuda_stream)
+{
+  ukg_clear_error();
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return ukg_set_error(KALMAN_GPU_ENODEV, "no CUDA device");
+  }
+  cudaStream_t st = (cudaStream_t)cuda_stream;
+  int* dflag = nullptr;
+  if (ukg_malloc_async((void**)&dflag, sizeof(int), st) != 0)
+    return ukg_set_error(KALMAN_GPU_ENOMEM, "allocating the check's flag failed");
+  int hflag = 0;
+  cudaMemsetAsync(dflag, 0, sizeof(int), st);
+  bounded_wait_check_kernel<<<1, 32, 0, st>>>(dflag);
+  cudaMemcpyAsync(&hflag, dflag, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(dflag, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return ukg_set_error(KALMAN_GPU_ECUDA, "bounded-wait check: %s", cudaGetErrorString(e));
+  if (hflag & 8) return ukg_set_error(KALMAN_GPU_ECUDA, "a bulk copy into shared memory did not complete in time");
+  return 0;
+}
+
 extern "C" int64_t kalman_gpu_oddeven_workspace_bytes(uint32_t options, const kalman_gpu_problem_t* p)
 {
   ukg_clear_error();

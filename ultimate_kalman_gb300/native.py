@@ -116,7 +116,7 @@ EXPORTED = [
     "kalman_gpu_plan_create", "kalman_gpu_plan_execute", "kalman_gpu_plan_status", "kalman_gpu_plan_destroy",
     "kalman_gpu_expand_invariant", "kalman_gpu_filter_packed", "kalman_gpu_oddeven_workspace_bytes",
     "kalman_gpu_workspace_held", "kalman_gpu_set_tuning", "kalman_gpu_get_tuning",
-    "kalman_gpu_smooth_oddeven_first_obs",
+    "kalman_gpu_smooth_oddeven_first_obs", "kalman_gpu_check_bounded_wait",
 ]
 
 _lib = None
@@ -151,6 +151,8 @@ def load(path=LIB_PATH):
     L.kalman_gpu_measure_fp64_tflops.argtypes = [ctypes.c_int]
     L.kalman_gpu_measure_fp64_tflops.restype = ctypes.c_double
     L.kalman_gpu_measure_fp32_tflops.restype = ctypes.c_double
+    L.kalman_gpu_check_bounded_wait.argtypes = [ctypes.c_void_p]
+    L.kalman_gpu_check_bounded_wait.restype = ctypes.c_int
     L.kalman_gpu_plan_create.argtypes = [ctypes.c_uint32, P]
     L.kalman_gpu_plan_create.restype = ctypes.c_void_p
     L.kalman_gpu_plan_execute.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
