@@ -927,11 +927,12 @@ __global__ void __launch_bounds__(BS ? BS : 1024) pair_kernel(Args<T, TI> a, int
 }
 
 /* ---------------------------------------------------------------------------
- * FP32 pair elimination with every block in registers.  The row counts of
- * stages A (m_j + n) and C (m_j + m_{j+1}) are dispatched at run time to
- * instantiations in which every loop bound is a compile-time constant, so the
- * pivot block P[col][row], the reflector scalars and the streamed column are
- * register arrays.  Same arithmetic as pair_kernel.
+ * Householder QR and reflector application on register arrays, for the FP32
+ * pair kernel below: the row counts of stages A (m_j + n) and C (m_j +
+ * m_{j+1}) are dispatched at run time to instantiations in which every loop
+ * bound is a compile-time constant, so the pivot block P[col][row], the
+ * reflector scalars and the streamed column are register arrays.  Same
+ * arithmetic as pair_kernel.
  * ------------------------------------------------------------------------ */
 template <int R, int C>
 __device__ __forceinline__ void hh_reg(float (&P)[C][R], float (&tau)[C])
@@ -985,186 +986,6 @@ __device__ __forceinline__ void apply_reg(const float (&P)[C][R], const float (&
   }
 }
 
-struct PairIdx {
-  int64_t sj, sj1, sn, se;
-};
-
-/* stage A with RA = m_j + N rows: pivot [G_j; F_{j+1}], rhs [o_j; c_{j+1}] */
-template <int N, int MX, int RA>
-__device__ __forceinline__ void reg_stage_a(const Args<float, float>& a, const PairIdx& x)
-{
-  constexpr int MJ = RA - N;
-  const Eq<float>& C = a.ce;
-  const Eq<float>& Nx = a.ne;
-  const Rec<float>& Rr = a.cr;
-  float P[N][RA], v[RA], tau[N];
-#pragma unroll
-  for (int q = 0; q < N; ++q) {
-#pragma unroll
-    for (int i = 0; i < MJ; ++i) P[q][i] = C.G.at(q * MX + i, x.sj);
-#pragma unroll
-    for (int i = 0; i < N; ++i) P[q][MJ + i] = C.F.at(q * N + i, x.sj1);
-  }
-#pragma unroll
-  for (int i = 0; i < MJ; ++i) v[i] = C.o.at(i, x.sj);
-#pragma unroll
-  for (int i = 0; i < N; ++i) v[MJ + i] = C.c.at(i, x.sj1);
-  hh_reg<RA, N>(P, tau);
-  apply_reg<RA, N>(P, tau, v);
-#pragma unroll
-  for (int q = 0; q < N; ++q)
-#pragma unroll
-    for (int i = 0; i < N; ++i) Rr.R.at(q * N + i, x.se) = (i <= q) ? P[q][i] : 0.0f;
-#pragma unroll
-  for (int i = 0; i < N; ++i) Rr.rhs.at(i, x.se) = v[i];
-#pragma unroll
-  for (int i = 0; i < MJ; ++i) Nx.o.at(i, x.sn) = v[N + i];
-#pragma unroll
-  for (int q = 0; q < N; ++q) {
-    float col[RA];
-#pragma unroll
-    for (int i = 0; i < MJ; ++i) col[i] = 0.0f;
-#pragma unroll
-    for (int i = 0; i < N; ++i) col[MJ + i] = C.H.at(q * N + i, x.sj1);
-    apply_reg<RA, N>(P, tau, col);
-#pragma unroll
-    for (int i = 0; i < N; ++i) Rr.Y.at(q * N + i, x.se) = col[i];
-#pragma unroll
-    for (int i = 0; i < MJ; ++i) Nx.G.at(q * MX + i, x.sn) = col[N + i];
-  }
-}
-
-/* stage C with RC = m_j + m_{j+1} rows: pivot [H~_{j+1}; G_{j+1}] */
-template <int N, int MX, int RC>
-__device__ __forceinline__ void reg_stage_c(const Args<float, float>& a, const PairIdx& x, int mj)
-{
-  const Eq<float>& C = a.ce;
-  const Eq<float>& Nx = a.ne;
-  float P[N][RC], v[RC], tau[N];
-#pragma unroll
-  for (int q = 0; q < N; ++q)
-#pragma unroll
-    for (int i = 0; i < RC; ++i) P[q][i] = i < mj ? Nx.G.at(q * MX + i, x.sn) : C.G.at(q * MX + (i - mj), x.sj1);
-#pragma unroll
-  for (int i = 0; i < RC; ++i) v[i] = i < mj ? Nx.o.at(i, x.sn) : C.o.at(i - mj, x.sj1);
-  hh_reg<RC, N>(P, tau);
-  apply_reg<RC, N>(P, tau, v);
-  constexpr int G = RC < N ? RC : N;
-#pragma unroll
-  for (int q = 0; q < N; ++q)
-#pragma unroll
-    for (int i = 0; i < G; ++i) Nx.G.at(q * MX + i, x.sn) = (i <= q) ? P[q][i] : 0.0f;
-#pragma unroll
-  for (int i = 0; i < G; ++i) Nx.o.at(i, x.sn) = v[i];
-  Nx.m[x.sn] = G;
-}
-
-/* stage B: pivot [H_j; R~_j] (2N rows) */
-template <int N, int MX>
-__device__ __forceinline__ void reg_stage_b(const Args<float, float>& a, const PairIdx& x)
-{
-  constexpr int R2 = 2 * N;
-  const Eq<float>& C = a.ce;
-  const Eq<float>& Nx = a.ne;
-  const Rec<float>& Rr = a.cr;
-  float P[N][R2], v[R2], tau[N];
-#pragma unroll
-  for (int q = 0; q < N; ++q)
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      P[q][i] = C.H.at(q * N + i, x.sj);
-      P[q][N + i] = Rr.R.at(q * N + i, x.se);
-    }
-#pragma unroll
-  for (int i = 0; i < N; ++i) {
-    v[i] = C.c.at(i, x.sj);
-    v[N + i] = Rr.rhs.at(i, x.se);
-  }
-  hh_reg<R2, N>(P, tau);
-  apply_reg<R2, N>(P, tau, v);
-#pragma unroll
-  for (int q = 0; q < N; ++q)
-#pragma unroll
-    for (int i = 0; i < N; ++i) Rr.R.at(q * N + i, x.se) = (i <= q) ? P[q][i] : 0.0f;
-#pragma unroll
-  for (int i = 0; i < N; ++i) {
-    Rr.rhs.at(i, x.se) = v[i];
-    Nx.c.at(i, x.sn) = v[N + i];
-  }
-#pragma unroll
-  for (int q = 0; q < N; ++q) {
-    float col[R2];
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      col[i] = C.F.at(q * N + i, x.sj);
-      col[N + i] = 0.0f;
-    }
-    apply_reg<R2, N>(P, tau, col);
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      Rr.Ft.at(q * N + i, x.se) = col[i];
-      Nx.F.at(q * N + i, x.sn) = col[N + i];
-    }
-  }
-#pragma unroll
-  for (int q = 0; q < N; ++q) {
-    float col[R2];
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      col[i] = 0.0f;
-      col[N + i] = Rr.Y.at(q * N + i, x.se);
-    }
-    apply_reg<R2, N>(P, tau, col);
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      Rr.Y.at(q * N + i, x.se) = col[i];
-      Nx.H.at(q * N + i, x.sn) = col[N + i];
-    }
-  }
-}
-
-template <int N, int MX, int RA = N>
-__device__ __forceinline__ void reg_dispatch_a(int ra, const Args<float, float>& a, const PairIdx& x)
-{
-  if constexpr (RA <= N + MX) {
-    if (ra == RA) reg_stage_a<N, MX, RA>(a, x);
-    else reg_dispatch_a<N, MX, RA + 1>(ra, a, x);
-  }
-}
-
-template <int N, int MX, int RC = 1>
-__device__ __forceinline__ void reg_dispatch_c(int rc, const Args<float, float>& a, const PairIdx& x, int mj)
-{
-  if constexpr (RC <= 2 * MX) {
-    if (rc == RC) reg_stage_c<N, MX, RC>(a, x, mj);
-    else reg_dispatch_c<N, MX, RC + 1>(rc, a, x, mj);
-  }
-}
-
-template <int N, int MX>
-__global__ void __launch_bounds__(128) pair_reg_kernel(Args<float, float> a, int)
-{
-  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (item >= a.ct.npairs) return;
-  const int t = find_track(a.ct.pair, a.ntracks, item);
-  const int64_t p = item - a.ct.pair[t];
-  PairIdx x;
-  x.sj = a.ct.slot[t] + 2 * p;
-  x.sj1 = x.sj + 1;
-  x.sn = a.nt.slot[t] + p;
-  x.se = a.ct.solve[t] + p;
-  const int mj = a.ce.m[x.sj], mj1 = a.ce.m[x.sj1];
-  reg_dispatch_a<N, MX>(mj + N, a, x);
-  if (mj + mj1 == 0) a.ne.m[x.sn] = 0;
-  else reg_dispatch_c<N, MX>(mj + mj1, a, x, mj);
-  if (p == 0) {
-#pragma unroll
-    for (int e = 0; e < N * N; ++e) a.cr.Ft.at(e, x.se) = 0.0f;
-    return;
-  }
-  reg_stage_b<N, MX>(a, x);
-}
-
 /* ---------------------------------------------------------------------------
  * FP32 pair elimination with the pair's inputs staged asynchronously.
  * Each thread copies its pair's level equations into its own slice of shared
@@ -1173,8 +994,7 @@ __global__ void __launch_bounds__(128) pair_reg_kernel(Args<float, float> a, int
  * the pair is in flight at once and stage A starts when its group lands.  The
  * intermediates (R~, rhs~, Y~, H~, o~) stay in the slice, over inputs already
  * consumed; records and the next level are written once.  Element e of
- * thread t's slice is at smem[e * BP + t] (no bank conflicts).  Same
- * arithmetic as pair_reg_kernel.
+ * thread t's slice is at smem[e * BP + t] (no bank conflicts).
  * ------------------------------------------------------------------------ */
 __device__ __forceinline__ void cp_async4(float* dst, const float* src)
 {
@@ -1198,6 +1018,7 @@ struct PairSlice {
   __device__ __forceinline__ float& operator[](int e) const { return t0[e * BP]; }
 };
 
+/* stage A with RA = m_j + N rows: pivot [G_j; F_{j+1}], rhs [o_j; c_{j+1}] */
 template <int N, int BP, int RA>
 __device__ __forceinline__ void ss_stage_a(const PairSlice<N, BP>& S)
 {
@@ -1242,6 +1063,7 @@ __device__ __forceinline__ void ss_stage_a(const PairSlice<N, BP>& S)
   }
 }
 
+/* stage C with RC = m_j + m_{j+1} rows: pivot [H~_{j+1}; G_{j+1}] */
 template <int N, int BP, int RC>
 __device__ __forceinline__ void ss_stage_c(const PairSlice<N, BP>& S, const Eq<float>& Nx, int64_t sn, int mj)
 {
@@ -1266,6 +1088,7 @@ __device__ __forceinline__ void ss_stage_c(const PairSlice<N, BP>& S, const Eq<f
   Nx.m[sn] = G;
 }
 
+/* stage B: pivot [H_j; R~_j] (2N rows) */
 template <int N, int BP>
 __device__ __forceinline__ void ss_stage_b(const PairSlice<N, BP>& S, const Eq<float>& Nx, const Rec<float>& Rr,
                                            int64_t sn, int64_t se)
@@ -3413,7 +3236,6 @@ extern "C" int64_t kalman_gpu_oddeven_workspace_bytes(uint32_t options, const ka
   if (p->nsteps == 0) return 0;
   const bool want_cov = !(options & KALMAN_NO_COVARIANCE) && p->covariance;
   const bool f32 = (options & KALMAN_GPU_FP32_REFINE) && !want_cov; /* with covariances: double-float, 8 bytes */
-  const int mxp = p->mmax > p->n ? p->mmax : p->n;
   Plan P;
   const kalman_gpu_tuning_t tune = tuning_now();
   const bool cta = use_cta(p, tune);
