@@ -82,8 +82,9 @@ def test_equals_the_padded_problem(location, form):
 
 @pytest.mark.gpu
 def test_host_arrays_in_several_staging_chunks():
-    """2.6 M steps: the host path stages about a million steps at a time, each
-    chunk with its own tracks' first observations."""
+    """2.6 M steps: the host path stages them in chunks of whole tracks (about
+    half a million steps each), each chunk with its own tracks' first
+    observations."""
     _gpu()
     P = pb.constant_velocity(pb.batched_lengths(260, 5000, 15000, seed=5), seed=6)
     assert P.nsteps > 2 * (1 << 20)

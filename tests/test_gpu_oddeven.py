@@ -83,7 +83,7 @@ def test_host_and_device_locations_agree():
 
 @pytest.mark.parametrize("fp32", [False, True])
 def test_host_location_in_pipelined_chunks(fp32):
-    """Host arrays of more than 2^20 steps are staged in chunks of whole tracks
+    """Host arrays of more than 2^19 steps are staged in chunks of whole tracks
     (copies overlapped with smoothing); the results equal the device path's."""
     P = pb.constant_velocity([600000, 600000, 100000, 37], seed=9)
     cov = not fp32
