@@ -392,25 +392,35 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                : "memory");
 }
 
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity)
+/* one potentially blocking wait on the phase: the thread may be suspended in
+ * hardware until the phase completes or a time limit of the implementation
+ * passes, instead of spending issue slots on polls                          */
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity)
 {
   uint32_t done;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
       : "=r"(done)
       : "r"(smem_u32(bar)), "r"(parity)
       : "memory");
   return done != 0;
 }
 
-/* polls the phase with a bound of about a second */
+__device__ __forceinline__ uint64_t global_ns()
+{
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+/* waits for the phase with a bound of one second of wall time */
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
 {
-  for (int it = 0; it < (1 << 23); ++it) {
-    if (mbar_test(bar, parity)) return true;
-    __nanosleep(100);
+  const uint64_t t0 = global_ns();
+  for (;;) {
+    if (mbar_try(bar, parity)) return true;
+    if (global_ns() - t0 > 1000000000ull) return false;
   }
-  return false;
 }
 
 /* the failure path of mbar_wait (kalman_gpu_check_bounded_wait): an mbarrier
