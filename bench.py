@@ -211,8 +211,10 @@ def roofline_for(prof, fl, steps, fp64_peak, fp32_peak, hbm_peak, compulsory_in,
     equations read once at their real sizes, flops.compulsory_bytes): they are
     credited to the kernel that reads the caller's equations (the weighing
     kernel); the other kernels move only intermediates, whose modelled bytes
-    are reported as traffic, not as algorithmic work.  FP64 kernels are placed
-    against the FP64 pipe when their flop fraction is the higher one."""
+    are reported as traffic, not as algorithmic work, and are placed against
+    their pipe with the flops of the model (flops.py: FP32 kernels against the
+    FP32 FMA peak, FP64 kernels against the FP64 one).  A kernel goes against
+    whichever of HBM and its pipe it is nearer to."""
     top = max(prof, key=lambda k: prof[k][0])
     kms, kl = prof[top]
     secs = kms * 1e-3 / steps
@@ -367,16 +369,26 @@ def run_gpu(args):
     peak32 = native.measure_fp32_tflops()
     peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(REPO, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
-    fl32 = {}  # the precision form is placed against HBM (see roofline_for)
+    # FP32 kernels against the FP32 FMA peak by the model's flops; the weighing (double-float
+    # arithmetic on the FP32 pipe, reading the caller's equations) against HBM by the compulsory bytes
+    fl32 = flops.plan_flops_fast_fp32(P.track_lengths(), 6, 3, sweeps=args.sweeps or 2)
+    fl32.pop("weigh_kernel")
     fl64 = flops.plan_flops_fast(P.track_lengths(), 6, 3, covariance=True)
     by32 = flops.plan_bytes_fast(P.track_lengths(), 6, 3, fp32=True, sweeps=args.sweeps or 2)
     by64 = flops.plan_bytes_fast(P.track_lengths(), 6, 3, fp32=False)
     comp = flops.compulsory_bytes(P.track_lengths(), 6, 3, covariance=False)
     comp_cov = flops.compulsory_bytes(P.track_lengths(), 6, 3, covariance=True)
     roof = roofline_for(prof, fl32, prof_steps, peak64, peak32, peaks["hbm_gbs"], comp[0], by32)
+    # the weighing kernel, which reads the caller's equations, against the compulsory bytes
+    # (the same object as `roofline` when the weighing is the longest kernel)
+    roof_w = roofline_for({k: v for k, v in prof.items() if k == "weigh_kernel"}, fl32, prof_steps, peak64, peak32,
+                          peaks["hbm_gbs"], comp[0], by32) if "weigh_kernel" in prof else None
     tfile = os.path.join(REPO, "profiles", "traffic_per_launch.json")
     if os.path.exists(tfile):
-        roof["traffic"] = json.load(open(tfile)).get(roof["kernel"])
+        traffic = json.load(open(tfile))
+        roof["traffic"] = traffic.get(roof["kernel"])
+        if roof_w:
+            roof_w["traffic"] = traffic.get("weigh_kernel")
     roof["per_kernel"] = {k: {"ms_per_step": v[0] / prof_steps, "launches_per_step": v[1] / prof_steps,
                               "share": v[0] / sum(x[0] for x in prof.values())} for k, v in prof.items()}
     roof64 = roofline_for(prof64, fl64, k2, peak64, peak32, peaks["hbm_gbs"], comp_cov[0], by64)
@@ -387,7 +399,8 @@ def run_gpu(args):
             "config": config_dict(P, args.tracks, world), "gpu_launches": int(launches),
             "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
                            "what": "one smoothing of all 4,096 tracks"},
-            "rel_err_vs_fp64": err, "roofline": roof, "whole_step": whole_step(comp, ms, peaks["hbm_gbs"]),
+            "rel_err_vs_fp64": err, "roofline": roof, "roofline_weighing": roof_w,
+            "whole_step": whole_step(comp, ms, peaks["hbm_gbs"]),
             "clocks": clocks,
             "plain_fp64": {"states_and_covariances": total_steps / (ms64c * 1e-3),
                            "states_only": total_steps / (ms64 * 1e-3), "unit": UNIT,
