@@ -513,9 +513,13 @@ void free_matrix(kalman_matrix_t* M)
   free(M);
 }
 
+/* a matrix the packing may read: elements present, leading dimension at least
+ * the row count */
+bool readable(const kalman_matrix_t* A) { return A && A->elements && A->ld >= A->row_dim && A->row_dim >= 0; }
+
 bool valid_cov(const kalman_matrix_t* Cm, char type, int dim)
 {
-  if (!Cm || !Cm->elements) return false;
+  if (!readable(Cm)) return false;
   if (type == 'w') return Cm->row_dim == dim && Cm->col_dim >= 1;
   if (type == 'W' || type == 'C' || type == 'U' || type == 'F') return Cm->row_dim == dim && Cm->col_dim == dim;
   return false;
@@ -621,7 +625,7 @@ int pack_equations(kalman_step_equations_t** eq, int64_t N, const kalman_step_in
     if (!first[s]) {
       const int np = eq[s - 1]->dimension, l = rows_of(e->H);
       if (l < 1 || l > n || cols_of(e->H) != ns || rows_of(e->F) != l || cols_of(e->F) != np || rows_of(e->c) != l ||
-          cols_of(e->c) != 1 || !e->H->elements || !e->F->elements || !e->c->elements)
+          cols_of(e->c) != 1 || !readable(e->H) || !readable(e->F) || !readable(e->c))
         return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld: H must be l x %d, F l x %d and c l x 1 with 1 <= l <= %d",
                              (long long)s, ns, np, n);
       if (!valid_cov(e->K, e->K_type, l))
@@ -631,8 +635,8 @@ int pack_equations(kalman_step_equations_t** eq, int64_t N, const kalman_step_in
     int m = 0;
     if (e->o) {
       m = rows_of(e->o);
-      if (m < 1 || cols_of(e->o) != 1 || rows_of(e->G) != m || cols_of(e->G) != ns || !e->G->elements ||
-          !e->o->elements)
+      if (m < 1 || cols_of(e->o) != 1 || rows_of(e->G) != m || cols_of(e->G) != ns || !readable(e->G) ||
+          !readable(e->o))
         return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld: G must be m x %d and o m x 1", (long long)s, ns);
       if (!valid_cov(e->C, e->C_type, m))
         return ukg_set_error(KALMAN_GPU_EINVAL, "step %lld: bad observation covariance (type '%c')", (long long)s,
@@ -799,9 +803,13 @@ extern "C" void kalman_smooth_associative(kalman_options_t options, kalman_step_
 extern "C" int kalman_gpu_smooth_tracks(uint32_t options, kalman_step_equations_t** equations,
                                         const kalman_step_index_t* track_lengths, int32_t ntracks)
 {
+  ukg_clear_error();
   if (ntracks < 1 || !track_lengths) return ukg_set_error(KALMAN_GPU_EINVAL, "no tracks");
   int64_t N = 0;
-  for (int t = 0; t < ntracks; ++t) N += track_lengths[t];
+  for (int t = 0; t < ntracks; ++t) {
+    if (track_lengths[t] < 0) return ukg_set_error(KALMAN_GPU_EINVAL, "negative track length");
+    N += track_lengths[t];
+  }
   const bool assoc = (options & KALMAN_ALGORITHM_ASSOCIATIVE) && !(options & KALMAN_ALGORITHM_ODDEVEN);
   return smooth_equations(assoc, options, equations, N, track_lengths, ntracks);
 }
@@ -819,9 +827,13 @@ struct kalman_st {
 
 namespace {
 
+/* a copy the library owns; NULL for a NULL or unreadable matrix (negative
+ * dimensions, no elements, leading dimension below the row count), which the
+ * smoothing then refuses as a missing block */
 kalman_matrix_t* copy_or_null(const kalman_matrix_t* A)
 {
-  if (!A) return nullptr;
+  if (!A || A->row_dim < 0 || A->col_dim < 0) return nullptr;
+  if (A->row_dim > 0 && A->col_dim > 0 && !readable(A)) return nullptr;
   kalman_matrix_t* B = new_matrix(A->row_dim, A->col_dim);
   for (int j = 0; j < A->col_dim; ++j)
     for (int i = 0; i < A->row_dim; ++i) B->elements[(size_t)j * B->ld + i] = A->elements[(size_t)j * A->ld + i];
