@@ -807,14 +807,32 @@ __global__ void __launch_bounds__(BS, 512 / BS) weigh_df_kernel(Args<float, floa
             default: hi = a.ce.o, lw = lo.o, stride = 0; break;
           }
           const bool negate = part == 2;
+          /* with an even leading dimension and block size every column starts on
+           * 16 bytes: read the staged column two entries at a time (half the
+           * shared-memory wavefronts of 8-byte loads at this thread stride).  The
+           * second entry of a pair past `rows` still lies in the step's block. */
+          const bool pairs = (MX % 2 == 0) && ((ld | per) & 1) == 0;
           for (int cc = 0; cc < ncols; ++cc) {
             df col[MX];
+            if (pairs) {
+              const double2* m2 = reinterpret_cast<const double2*>(mine + cc * ld);
 #pragma unroll
-            for (int r = 0; r < MX; ++r) {
-              col[r] = make(0.0f);
-              if (r < rows) col[r] = split(mine[cc * ld + r]);
-              if (negate) col[r] = neg(col[r]);
+              for (int r = 0; r < MX; r += 2) {
+                double2 w = make_double2(0.0, 0.0);
+                if (r < rows) w = m2[r / 2];
+                col[r] = r < rows ? split(w.x) : make(0.0f);
+                if (r + 1 < MX) col[r + 1] = r + 1 < rows ? split(w.y) : make(0.0f);
+              }
+            } else {
+#pragma unroll
+              for (int r = 0; r < MX; ++r) {
+                col[r] = make(0.0f);
+                if (r < rows) col[r] = split(mine[cc * ld + r]);
+              }
             }
+            if (negate)
+#pragma unroll
+              for (int r = 0; r < MX; ++r) col[r] = neg(col[r]);
             V.apply(col);
 #pragma unroll
             for (int r = 0; r < MX; ++r) {
