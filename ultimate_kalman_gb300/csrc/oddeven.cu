@@ -2287,16 +2287,58 @@ __global__ void __launch_bounds__(128) rt_odd_reg_kernel(Args<float, float> a, S
   }
 }
 
+/* rt_base_kernel with the track's base-case R and right-hand side in
+ * registers: the same two triangular solves in the same order (the results
+ * are identical), without a round trip to memory per operation.            */
+template <int N>
+__global__ void __launch_bounds__(128) rt_base_reg_kernel(Args<float, float> a, Soa<float> zc)
+{
+  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= a.ct.ntail) return;
+  const int t = (int)a.ct.tail[item];
+  if (a.ct.L[t] != 1) return;
+  const int64_t sz = a.ct.slot[t];
+  float R[N][N], v[N]; /* R[j][i]: row i of column j, i <= j */
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    v[j] = zc.at(j, sz);
+#pragma unroll
+    for (int i = 0; i <= j; ++i) R[j][i] = a.baseR.at(j * N + i, t);
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) { /* R^T y = z */
+    float sm = v[i];
+#pragma unroll
+    for (int k = 0; k < i; ++k) sm = fmaf(-R[i][k], v[k], sm);
+    v[i] = sm * (1.0f / R[i][i]);
+  }
+#pragma unroll
+  for (int j = N - 1; j >= 0; --j) { /* R d = y */
+    const float xj = v[j] * (1.0f / R[j][j]);
+    v[j] = xj;
+#pragma unroll
+    for (int i = 0; i < j; ++i) v[i] = fmaf(-xj, R[j][i], v[i]);
+  }
+  double* d = a.state + orig_step(a.track_start, a.level, t, 0) * N;
+#pragma unroll
+  for (int i = 0; i < N; ++i) d[i] = ukg_df::f32_to_f64(v[i]);
+}
+
 struct RegSolves {
   void (*solve)(Args<float, float>) = nullptr;
   void (*rt_even)(Args<float, float>, Soa<float>, Soa<float>) = nullptr;
   void (*rt_odd)(Args<float, float>, Soa<float>, Soa<float>, Soa<float>) = nullptr;
+  void (*rt_base)(Args<float, float>, Soa<float>) = nullptr;
 };
 RegSolves reg_solves(int n)
 {
   RegSolves r;
-  if (n == 6) r.solve = solve_state_reg_kernel<6>, r.rt_even = rt_even_reg_kernel<6>, r.rt_odd = rt_odd_reg_kernel<6>;
-  if (n == 4) r.solve = solve_state_reg_kernel<4>, r.rt_even = rt_even_reg_kernel<4>, r.rt_odd = rt_odd_reg_kernel<4>;
+  if (n == 6)
+    r.solve = solve_state_reg_kernel<6>, r.rt_even = rt_even_reg_kernel<6>, r.rt_odd = rt_odd_reg_kernel<6>,
+    r.rt_base = rt_base_reg_kernel<6>;
+  if (n == 4)
+    r.solve = solve_state_reg_kernel<4>, r.rt_even = rt_even_reg_kernel<4>, r.rt_odd = rt_odd_reg_kernel<4>,
+    r.rt_base = rt_base_reg_kernel<4>;
   return r;
 }
 
@@ -2816,7 +2858,10 @@ int run_plan(uint32_t options, const kalman_gpu_problem_t* p, cudaStream_t st, c
         }
         if (lp[l].ntail > 0) {
           Soa<float> tmp{(float*)(B + P.o_tmp), std::max(T_, 1)};
-          UKG_LAUNCH(UKG_K_RT, st, (rt_base_kernel<<<grid(lp[l].ntail, 128), 128, 0, st>>>(a, zc, tmp)));
+          if (RS.rt_base)
+            UKG_LAUNCH(UKG_K_RT, st, (RS.rt_base<<<grid(lp[l].ntail, 128), 128, 0, st>>>(a, zc)));
+          else
+            UKG_LAUNCH(UKG_K_RT, st, (rt_base_kernel<<<grid(lp[l].ntail, 128), 128, 0, st>>>(a, zc, tmp)));
         }
       }
       for (int l = nlev - 2; l >= 0; --l) {
